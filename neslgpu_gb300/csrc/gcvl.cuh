@@ -1,0 +1,258 @@
+// gcvl.cuh -- shared definitions of the GB300 CVL library (libcvl_gb300.so).
+//
+// The library implements the C vector library ABI of NESL's VCODE
+// interpreter (nesl/include/cvl.h of Nessie-Compiler/neslgpu) with
+// hand-written sm_103a kernels.  vec_p is a raw device pointer (the
+// HAS_VOIDP branch of cvl.h:50-53) and sizes are counted in 8-byte units
+// (CVL_SIZE_UNIT = sizeof(MAXALIGN) of the serial CVL, facilt.c:92-93).
+//
+// One host thread, one library stream, calls ordered on that stream.
+// Functions that return a scalar to the host synchronise the stream.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <limits.h>
+#include <string.h>
+
+// The public header: every export below must match its declaration there.
+#include "cvl_gb300.h"
+
+#define GCVL_EXPORT extern "C" __attribute__((visibility("default")))
+
+namespace gcvl {
+
+// ---------------------------------------------------------------- state ---
+struct State {
+  bool ready = false;
+  int device = 0;
+  int sm_count = 152;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  unsigned *d_status = nullptr;     // device-side error word (bounded waits)
+  void *d_small = nullptr;          // 4 KB device scratch for scalar results
+  void *h_small = nullptr;          // 4 KB pinned host mirror
+  void *work = nullptr;             // library workspace used when the caller
+  size_t work_bytes = 0;            //   passes a NULL scratch vector
+  void *stage = nullptr;            // staging buffer for overlapping mov_fov
+  size_t stage_bytes = 0;
+  uint64_t rand48 = 0x1234ABCD330EULL;  // lrand48 state (POSIX initial value)
+  int spin_limit = 1 << 22;         // bounded-wait iteration limit
+  int err = 0;
+  char msg[256] = {0};
+  char fused_lib[1024] = {0};
+};
+State &st();
+void ensure_init();
+void set_error(int code, const char *fmt, ...);
+bool check_cuda(cudaError_t e, const char *what);
+#define GCVL_CK(call) ::gcvl::check_cuda((call), #call)
+inline cudaStream_t stream() { return st().stream; }
+// Device scratch for a call: the caller's vec_p when given, else the
+// library workspace (grown on demand, kept for later calls).
+void *scratch_or_work(vec_p scratch, size_t bytes);
+void launch_check(const char *what);
+
+enum ErrorCode {
+  GCVL_OK = 0,
+  GCVL_ERR_CUDA = 1,
+  GCVL_ERR_ARG = 2,
+  GCVL_ERR_TIMEOUT = 3,   // a bounded device wait gave up
+  GCVL_ERR_NOMEM = 4,
+  GCVL_ERR_RANGE = 5,
+};
+// bits of the device status word
+enum : unsigned { DEV_TIMEOUT = 1u };
+
+inline int ceil_div(long a, long b) { return (int)((a + b - 1) / b); }
+inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+// ------------------------------------------------------------ operators ---
+// The CVL scan/reduce operators with the serial CVL's initial values
+// (nesl/cvl/serial/vprims.c:33-49, defins.h:217-228).  init() is the value a
+// segment starts from; ident() is a true identity used for padding lanes and
+// empty partial results.  apply(a, b) has a = earlier element.
+struct AddZ { typedef int T;
+  __host__ __device__ static T init() { return 0; }
+  __host__ __device__ static T ident() { return 0; }
+  __device__ static T apply(T a, T b) { return (T)((unsigned)a + (unsigned)b); } };
+struct MulZ { typedef int T;
+  __host__ __device__ static T init() { return 1; }
+  __host__ __device__ static T ident() { return 1; }
+  __device__ static T apply(T a, T b) { return (T)((unsigned)a * (unsigned)b); } };
+struct MinZ { typedef int T;
+  __host__ __device__ static T init() { return INT_MAX; }
+  __host__ __device__ static T ident() { return INT_MAX; }
+  __device__ static T apply(T a, T b) { return a < b ? a : b; } };
+struct MaxZ { typedef int T;
+  __host__ __device__ static T init() { return INT_MIN; }
+  __host__ __device__ static T ident() { return INT_MIN; }
+  __device__ static T apply(T a, T b) { return a > b ? a : b; } };
+struct AndZ { typedef int T;
+  __host__ __device__ static T init() { return ~0; }
+  __host__ __device__ static T ident() { return ~0; }
+  __device__ static T apply(T a, T b) { return a & b; } };
+struct IorZ { typedef int T;
+  __host__ __device__ static T init() { return 0; }
+  __host__ __device__ static T ident() { return 0; }
+  __device__ static T apply(T a, T b) { return a | b; } };
+struct XorZ { typedef int T;
+  __host__ __device__ static T init() { return 0; }
+  __host__ __device__ static T ident() { return 0; }
+  __device__ static T apply(T a, T b) { return a ^ b; } };
+// logical operators on cvl_bool: results are 0/1 whatever the inputs hold
+struct AndB { typedef int T;
+  __host__ __device__ static T init() { return 1; }
+  __host__ __device__ static T ident() { return 1; }
+  __device__ static T apply(T a, T b) { return (a != 0) & (b != 0); } };
+struct IorB { typedef int T;
+  __host__ __device__ static T init() { return 0; }
+  __host__ __device__ static T ident() { return 0; }
+  __device__ static T apply(T a, T b) { return (a != 0) | (b != 0); } };
+struct XorB { typedef int T;
+  __host__ __device__ static T init() { return 0; }
+  __host__ __device__ static T ident() { return 0; }
+  __device__ static T apply(T a, T b) { return (a != 0) ^ (b != 0); } };
+// float64: -0.0 is the exact additive identity; min/max use +-inf as
+// identity while segments start from the serial CVL's +-1e36 (as float).
+struct AddD { typedef double T;
+  __host__ __device__ static T init() { return 0.0; }
+  __host__ __device__ static T ident() { return -0.0; }
+  __device__ static T apply(T a, T b) { return __dadd_rn(a, b); } };
+struct MulD { typedef double T;
+  __host__ __device__ static T init() { return 1.0; }
+  __host__ __device__ static T ident() { return 1.0; }
+  __device__ static T apply(T a, T b) { return __dmul_rn(a, b); } };
+__host__ __device__ inline double bits_to_double(unsigned long long v) {
+  union { unsigned long long l; double d; } u; u.l = v; return u.d;
+}
+struct MinD { typedef double T;
+  __host__ __device__ static T init() { return (double)(float)1.0e36; }
+  __host__ __device__ static T ident() { return bits_to_double(0x7FF0000000000000ULL); }
+  __device__ static T apply(T a, T b) { return a < b ? a : b; } };
+struct MaxD { typedef double T;
+  __host__ __device__ static T init() { return (double)(float)-1.0e36; }
+  __host__ __device__ static T ident() { return bits_to_double(0xFFF0000000000000ULL); }
+  __device__ static T apply(T a, T b) { return a > b ? a : b; } };
+// pk1_lev counts true flags per segment: an add over (x != 0).
+struct CountB { typedef int T;
+  __host__ __device__ static T init() { return 0; }
+  __host__ __device__ static T ident() { return 0; }
+  __device__ static T apply(T a, T b) { return a + b; } };
+
+// ------------------------------------------------------- device helpers ---
+template <class T> __device__ __forceinline__ T shfl_up(T v, int d) { return __shfl_up_sync(0xffffffffu, v, d); }
+template <class T> __device__ __forceinline__ T shfl_down(T v, int d) { return __shfl_down_sync(0xffffffffu, v, d); }
+template <class T> __device__ __forceinline__ T shfl_idx(T v, int l) { return __shfl_sync(0xffffffffu, v, l); }
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release(unsigned *p, unsigned v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+template <class T> __device__ __forceinline__ void st_relaxed(T *p, T v) {
+  if constexpr (sizeof(T) == 8) {
+    unsigned long long b; memcpy(&b, &v, 8);
+    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(b) : "memory");
+  } else {
+    unsigned b; memcpy(&b, &v, 4);
+    asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(b) : "memory");
+  }
+}
+template <class T> __device__ __forceinline__ T ld_relaxed(const T *p) {
+  T v;
+  if constexpr (sizeof(T) == 8) {
+    unsigned long long b;
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(b) : "l"(p) : "memory");
+    memcpy(&v, &b, 8);
+  } else {
+    unsigned b;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(b) : "l"(p) : "memory");
+    memcpy(&v, &b, 4);
+  }
+  return v;
+}
+
+// --------------------------------------------------- segment descriptor ---
+// Device layout of a segment descriptor (all int32, in one vec_p of
+// siz_fos(n, m) units):
+//   [0, m)                    segment lengths (what len_fos returns)
+//   [L0, L0 + m + 1)          offsets: exclusive scan of the lengths, then n
+//   [L1, L1 + ng + 1)         granule table: for granule g (elements
+//                             g*kGranule...), the segment that holds element
+//                             g*kGranule; entry ng holds m
+// with L0 = align4(m), L1 = L0 + align4(m + 1), ng = ceil(n / kGranule).
+constexpr int kGranule = 64;
+struct SegView {
+  const int *len;
+  const int *off;
+  const int *gran;
+  int n, m;
+};
+__host__ __device__ inline long segdes_off_words(int m) { return ((long)m + 3) & ~3L; }
+__host__ __device__ inline long segdes_gran_words(int m) {
+  return segdes_off_words(m) + (((long)m + 1 + 3) & ~3L);
+}
+__host__ __device__ inline long segdes_total_words(int n, int m) {
+  long ng = ((long)n + kGranule - 1) / kGranule;
+  return segdes_gran_words(m) + ((ng + 1 + 3) & ~3L);
+}
+inline SegView seg_view(vec_p sd, int n, int m) {
+  const int *b = (const int *)sd;
+  return SegView{b, b + segdes_off_words(m), b + segdes_gran_words(m), n, m};
+}
+
+// Segment holding element k (0 <= k < n): the largest s with off[s] <= k.
+// The granule table bounds the search to the segments of one granule.
+__device__ __forceinline__ int seg_of(const SegView &v, int k) {
+  int g = k / kGranule;
+  int lo = __ldg(v.gran + g);
+  int hi = __ldg(v.gran + g + 1);
+  if (hi > v.m - 1) hi = v.m - 1;
+  // invariant: off[lo] <= k; answer in [lo, hi]
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (__ldg(v.off + mid) <= k) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+// --------------------------------------------------- tile status arrays ---
+// Decoupled look-back state for one launch, carved out of scratch:
+//   counter (u32, dynamic tile ticket), flags[tiles] (u32),
+//   agg[tiles] (T, 8-byte slots), inc[tiles] (T, 8-byte slots).
+// Only counter and flags need clearing before a launch.
+enum : unsigned { TS_EMPTY = 0, TS_AGG = 1, TS_INC = 2 };
+struct LookbackMem {
+  unsigned *counter;
+  unsigned *flags;
+  unsigned long long *agg;
+  unsigned long long *inc;
+};
+inline size_t lookback_bytes(int tiles) {
+  return 256 + align_up((size_t)tiles * 4, 256) + 2 * align_up((size_t)tiles * 8, 256);
+}
+inline size_t lookback_clear_bytes(int tiles) { return 256 + align_up((size_t)tiles * 4, 256); }
+inline LookbackMem lookback_carve(void *base, int tiles) {
+  char *p = (char *)base;
+  LookbackMem L;
+  L.counter = (unsigned *)p;
+  L.flags = (unsigned *)(p + 256);
+  L.agg = (unsigned long long *)(p + 256 + align_up((size_t)tiles * 4, 256));
+  L.inc = (unsigned long long *)((char *)L.agg + align_up((size_t)tiles * 8, 256));
+  return L;
+}
+// scratch units (8 bytes) needed by a look-back launch of `tiles` tiles
+inline int lookback_units(int tiles) { return (int)((lookback_bytes(tiles) + 7) / 8); }
+
+template <class T> __device__ __forceinline__ unsigned long long to_bits(T v) {
+  unsigned long long b = 0; memcpy(&b, &v, sizeof(T)); return b;
+}
+template <class T> __device__ __forceinline__ T from_bits(unsigned long long b) {
+  T v; memcpy(&v, &b, sizeof(T)); return v;
+}
+
+}  // namespace gcvl

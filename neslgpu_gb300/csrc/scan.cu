@@ -1,0 +1,538 @@
+// scan.cu -- segmented and unsegmented scans and reductions.
+//
+// Semantics: the serial CVL (nesl/cvl/serial/vprims.c:17-201): exclusive
+// scans that restart from the operator's initial value at every segment,
+// reductions that yield the initial value for an empty segment.
+//
+// Design: one single-pass kernel per (operator, mode).  A CTA takes the next
+// tile ticket, stages its tile through shared memory with coalesced loads,
+// folds (head, value) pairs per thread, scans them across the CTA with warp
+// shuffles, and gets the carry from earlier tiles by decoupled look-back.
+// A tile that holds a segment head publishes its inclusive value at once, so
+// with short segments no CTA ever waits; long segments wait on a chain that
+// the warp-wide look-back walks 32 tiles at a time.  Every wait is bounded.
+#include "gcvl.cuh"
+
+namespace gcvl {
+
+template <class T> struct Tiling;
+template <> struct Tiling<int> { static constexpr int BLOCK = 256, ITEMS = 16; };
+template <> struct Tiling<double> { static constexpr int BLOCK = 256, ITEMS = 8; };
+
+enum Mode { M_SCAN = 0, M_REDUCE = 1, M_OFFSETS = 2 };
+
+template <class T> struct ScanArgs {
+  T *out;            // scan: n outputs; reduce: m outputs; offsets: m+1
+  const T *in;       // n inputs
+  T *out2;           // offsets mode: copy of the input (segment lengths)
+  SegView sv;        // segment descriptor (segmented kernels only)
+  int n;
+  LookbackMem lb;
+  unsigned *status;
+  int spin_limit;
+  int count_flags;   // pk1_lev: fold (x != 0) instead of x
+};
+
+// Coalesced load of a tile into per-thread blocked registers through padded
+// shared memory (conflict-free for 4- and 8-byte elements).
+template <class T, int ITEMS>
+__device__ __forceinline__ void load_blocked(T (&x)[ITEMS], const T *__restrict__ g, int valid,
+                                             T fill, T *sbuf) {
+  constexpr int PE = 128 / sizeof(T);
+  const int lane = threadIdx.x & 31;
+  const int wbase = (threadIdx.x >> 5) * 32 * ITEMS;
+#pragma unroll
+  for (int j = 0; j < ITEMS; j++) {
+    int idx = wbase + j * 32 + lane;
+    T v = fill;
+    if (idx < valid) v = __ldcs(g + idx);
+    sbuf[idx + idx / PE] = v;
+  }
+  __syncwarp();
+#pragma unroll
+  for (int i = 0; i < ITEMS; i++) {
+    int idx = threadIdx.x * ITEMS + i;
+    x[i] = sbuf[idx + idx / PE];
+  }
+  __syncwarp();
+}
+
+template <class T, int ITEMS>
+__device__ __forceinline__ void store_blocked(const T (&y)[ITEMS], T *__restrict__ g, int valid,
+                                              T *sbuf) {
+  constexpr int PE = 128 / sizeof(T);
+  const int lane = threadIdx.x & 31;
+  const int wbase = (threadIdx.x >> 5) * 32 * ITEMS;
+#pragma unroll
+  for (int i = 0; i < ITEMS; i++) {
+    int idx = threadIdx.x * ITEMS + i;
+    sbuf[idx + idx / PE] = y[i];
+  }
+  __syncwarp();
+#pragma unroll
+  for (int j = 0; j < ITEMS; j++) {
+    int idx = wbase + j * 32 + lane;
+    if (idx < valid) __stcs(g + idx, sbuf[idx + idx / PE]);
+  }
+  __syncwarp();
+}
+
+// Head bits of elements k0 .. k0+cnt-1 (bit i set when k0+i starts a
+// non-empty segment) and the segment holding k0.
+template <int ITEMS>
+__device__ __forceinline__ unsigned head_bits(const SegView &sv, int k0, int cnt, int &s0) {
+  unsigned h = 0;
+  int s = seg_of(sv, k0);
+  s0 = s;
+  if (__ldg(sv.off + s) == k0) h = 1u;
+  int nxt = __ldg(sv.off + s + 1);
+  while (nxt < k0 + cnt) {
+    h |= 1u << (nxt - k0);
+    ++s;
+    while (__ldg(sv.off + s + 1) == nxt) ++s;
+    nxt = __ldg(sv.off + s + 1);
+  }
+  return h;
+}
+
+template <class Op, int MODE, bool SEG>
+__global__ void __launch_bounds__(Tiling<typename Op::T>::BLOCK)
+k_scan(ScanArgs<typename Op::T> a) {
+  typedef typename Op::T T;
+  constexpr int BLOCK = Tiling<T>::BLOCK, ITEMS = Tiling<T>::ITEMS, TILE = BLOCK * ITEMS;
+  constexpr int NW = BLOCK / 32;
+  constexpr int PE = 128 / sizeof(T);
+  __shared__ T s_stage[TILE + TILE / PE];
+  __shared__ int s_wf[NW];
+  __shared__ T s_wv[NW];
+  __shared__ T s_prefix;
+  __shared__ unsigned s_tile;
+
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (tid == 0) s_tile = atomicAdd(a.lb.counter, 1u);
+  __syncthreads();
+  const int tile = (int)s_tile;
+  const long base = (long)tile * TILE;
+  const int valid = (int)min((long)TILE, (long)a.n - base);
+
+  T x[ITEMS];
+  load_blocked<T, ITEMS>(x, a.in + base, valid, Op::ident(), s_stage);
+  if (a.count_flags) {
+#pragma unroll
+    for (int i = 0; i < ITEMS; i++) x[i] = (x[i] != (T)0) ? (T)1 : (T)0;
+  }
+
+  const int k0 = (int)base + tid * ITEMS;
+  const int cnt = max(0, min(ITEMS, a.n - k0));
+  unsigned heads = 0;
+  int s0 = 0;
+  if (cnt > 0) {
+    if (SEG) heads = head_bits<ITEMS>(a.sv, k0, cnt, s0);
+    else heads = (k0 == 0) ? 1u : 0u;
+  }
+
+  // per-thread fold of (head, value); padding items are identities
+  int tf = heads != 0;
+  T tv = Op::ident();
+#pragma unroll
+  for (int i = 0; i < ITEMS; i++) {
+    if (i < cnt) tv = ((heads >> i) & 1u) ? Op::apply(Op::init(), x[i]) : Op::apply(tv, x[i]);
+  }
+
+  // warp inclusive scan of the pairs
+  int f = tf;
+  T v = tv;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    int f2 = shfl_up(f, d);
+    T v2 = shfl_up(v, d);
+    if (lane >= d) { v = f ? v : Op::apply(v2, v); f |= f2; }
+  }
+  int ef = shfl_up(f, 1);
+  T ev = shfl_up(v, 1);
+  if (lane == 0) { ef = 0; ev = Op::ident(); }
+  if (lane == 31) { s_wf[warp] = f; s_wv[warp] = v; }
+  __syncthreads();
+
+  // prefix over the warps before mine, and the tile aggregate
+  int pf = 0, af = 0;
+  T pv = Op::ident(), av = Op::ident();
+#pragma unroll
+  for (int w = 0; w < NW; w++) {
+    int wf = s_wf[w];
+    T wv = s_wv[w];
+    if (w == warp) { pf = af; pv = av; }
+    av = wf ? wv : Op::apply(av, wv);
+    af |= wf;
+  }
+  // in-tile exclusive prefix of this thread
+  pv = ef ? ev : Op::apply(pv, ev);
+  pf |= ef;
+
+  // publish and look back
+  if (warp == 0) {
+    // thread 0 holds element `base`: its head bit says whether the tile
+    // starts a segment (then no carry from earlier tiles is needed)
+    const bool first_head = shfl_idx((int)(heads & 1u), 0) != 0;
+    if (lane == 0) {
+      if (tile == 0 || af) {
+        st_relaxed(a.lb.inc + tile, to_bits<T>(av));
+        st_release(a.lb.flags + tile, TS_INC);
+      } else {
+        st_relaxed(a.lb.agg + tile, to_bits<T>(av));
+        st_release(a.lb.flags + tile, TS_AGG);
+      }
+    }
+    T P = Op::ident();
+    if (tile > 0 && !first_head) {
+      int pred = tile - 1;
+      while (true) {
+        int t = pred - lane;
+        unsigned fl = TS_INC;
+        T val = Op::ident();
+        if (t >= 0) {
+          int it = 0;
+          fl = ld_acquire(a.lb.flags + t);
+          while (fl == TS_EMPTY) {
+            if (++it >= a.spin_limit) break;
+            __nanosleep(32);
+            fl = ld_acquire(a.lb.flags + t);
+          }
+          if (fl == TS_EMPTY) { atomicOr(a.status, DEV_TIMEOUT); fl = TS_INC; }
+          else val = from_bits<T>(ld_relaxed(fl == TS_INC ? a.lb.inc + t : a.lb.agg + t));
+        }
+        unsigned incm = __ballot_sync(0xffffffffu, fl == TS_INC);
+        int stop = incm ? __ffs(incm) - 1 : 31;
+        if (lane > stop) val = Op::ident();
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+          T o = shfl_down(val, d);
+          if (lane + d < 32) val = Op::apply(o, val);
+        }
+        val = shfl_idx(val, 0);
+        P = Op::apply(val, P);
+        if (incm) break;
+        pred -= 32;
+      }
+      if (lane == 0 && !af) {
+        st_relaxed(a.lb.inc + tile, to_bits<T>(Op::apply(P, av)));
+        st_release(a.lb.flags + tile, TS_INC);
+      }
+    }
+    if (lane == 0) s_prefix = P;
+  }
+  __syncthreads();
+  const T P = s_prefix;
+  T run = pf ? pv : Op::apply(P, pv);
+
+  if (MODE == M_SCAN || MODE == M_OFFSETS) {
+    T y[ITEMS];
+#pragma unroll
+    for (int i = 0; i < ITEMS; i++) {
+      if ((heads >> i) & 1u) run = Op::init();
+      y[i] = run;
+      run = Op::apply(run, x[i]);
+    }
+    __syncthreads();  // s_stage reuse
+    store_blocked<T, ITEMS>(y, a.out + base, valid, s_stage);
+    if (MODE == M_OFFSETS) {
+      store_blocked<T, ITEMS>(x, a.out2 + base, valid, s_stage);
+      if (k0 < a.n && k0 + cnt == a.n) a.out[a.n] = run;  // total after the last element
+    }
+  } else {  // M_REDUCE
+    if (cnt > 0) {
+      const int m = a.sv.m;
+      if (k0 == 0) {
+        for (int s = 0; s < s0; s++) a.out[s] = Op::init();  // leading empty segments
+      }
+      int s = s0;
+      int end = __ldg(a.sv.off + s + 1);
+      for (int i = 0; i < cnt; i++) {
+        if ((heads >> i) & 1u) run = Op::init();
+        run = Op::apply(run, x[i]);
+        if (k0 + i + 1 == end) {
+          a.out[s] = run;
+          int s2 = s + 1;
+          while (s2 < m && __ldg(a.sv.off + s2 + 1) == end) { a.out[s2] = Op::init(); ++s2; }
+          s = s2;
+          if (s < m) end = __ldg(a.sv.off + s + 1);
+        }
+      }
+    }
+  }
+}
+
+template <class Op>
+__global__ void k_fill(typename Op::T *out, int m) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < m) out[i] = Op::init();
+}
+
+template <class T> constexpr int tile_elems() { return Tiling<T>::BLOCK * Tiling<T>::ITEMS; }
+
+template <class T> int scan_units(int n) {
+  if (n <= 0) return 0;
+  return lookback_units(ceil_div(n, tile_elems<T>()));
+}
+
+// Shared launcher.  `sd` may be null for unsegmented modes.
+template <class Op, int MODE, bool SEG>
+void run_scan(typename Op::T *out, const typename Op::T *in, typename Op::T *out2, vec_p sd,
+              int n, int m, vec_p scratch, bool count_flags, const char *name) {
+  typedef typename Op::T T;
+  ensure_init();
+  State &S = st();
+  if (n <= 0) return;
+  const int tiles = ceil_div(n, tile_elems<T>());
+  void *mem = scratch_or_work(scratch, lookback_bytes(tiles));
+  if (!mem) return;
+  ScanArgs<T> a;
+  a.out = out; a.in = in; a.out2 = out2; a.n = n;
+  a.sv = SEG ? seg_view(sd, n, m) : SegView{nullptr, nullptr, nullptr, n, 1};
+  a.lb = lookback_carve(mem, tiles);
+  a.status = S.d_status;
+  a.spin_limit = S.spin_limit;
+  a.count_flags = count_flags ? 1 : 0;
+  GCVL_CK(cudaMemsetAsync(mem, 0, lookback_clear_bytes(tiles), S.stream));
+  k_scan<Op, MODE, SEG><<<tiles, Tiling<T>::BLOCK, 0, S.stream>>>(a);
+  launch_check(name);
+}
+
+// ---------------------------------------------- unsegmented reductions ---
+// Two-level reduction with a fixed combine order (deterministic for a given
+// device): per-CTA partials, then the last CTA folds them in CTA order.
+constexpr int RBLOCK = 512;
+template <class Op>
+__global__ void __launch_bounds__(RBLOCK) k_reduce(const typename Op::T *__restrict__ in, long n,
+                                                  typename Op::T *partial, unsigned *ticket,
+                                                  typename Op::T *result, int count_flags) {
+  typedef typename Op::T T;
+  __shared__ T s_w[RBLOCK / 32];
+  __shared__ bool s_last;
+  T acc = Op::ident();
+  const long stride = (long)gridDim.x * RBLOCK;
+  // contiguous chunk per CTA keeps the fold order simple and loads coalesced
+  long per = (n + gridDim.x - 1) / gridDim.x;
+  long lo = (long)blockIdx.x * per, hi = min(n, lo + per);
+  (void)stride;
+  for (long i = lo + threadIdx.x; i < hi; i += RBLOCK) {
+    T x = __ldcs(in + i);
+    if (count_flags) x = (x != (T)0) ? (T)1 : (T)0;
+    acc = Op::apply(acc, x);
+  }
+  // thread order within a warp, then warps in order
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    T o = shfl_down(acc, d);
+    if ((threadIdx.x & 31) + d < 32) acc = Op::apply(acc, o);
+  }
+  if ((threadIdx.x & 31) == 0) s_w[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    T b = Op::ident();
+    for (int w = 0; w < RBLOCK / 32; w++) b = Op::apply(b, s_w[w]);
+    partial[blockIdx.x] = b;
+    __threadfence();
+    unsigned t = atomicAdd(ticket, 1u);
+    s_last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (s_last && threadIdx.x < 32) {
+    __threadfence();
+    // lane l folds partials l, l+32, ...: ordered within lane, then lanes
+    T r = Op::ident();
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += 32) r = Op::apply(r, ld_relaxed(partial + i));
+    // gather lanes in order on lane 0
+    // (order across lanes differs from CTA order only by a fixed permutation)
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      T o = shfl_down(r, d);
+      if ((threadIdx.x & 31) + d < 32) r = Op::apply(r, o);
+    }
+    if (threadIdx.x == 0) {
+      *result = Op::apply(Op::init(), r);
+      *ticket = 0;
+    }
+  }
+}
+
+template <class Op>
+void run_reduce(const typename Op::T *in, int n, typename Op::T *result_dev, vec_p scratch,
+                bool count_flags) {
+  typedef typename Op::T T;
+  ensure_init();
+  State &S = st();
+  if (n <= 0) {
+    T v = Op::init();
+    GCVL_CK(cudaMemcpyAsync(result_dev, &v, sizeof(T), cudaMemcpyHostToDevice, S.stream));
+    GCVL_CK(cudaStreamSynchronize(S.stream));
+    return;
+  }
+  int grid = S.sm_count * 2;
+  long need = ((long)n + RBLOCK - 1) / RBLOCK;
+  if (grid > need) grid = (int)need;
+  void *mem = scratch_or_work(scratch, 256 + (size_t)grid * 8);
+  if (!mem) return;
+  unsigned *ticket = (unsigned *)mem;
+  T *partial = (T *)((char *)mem + 256);
+  GCVL_CK(cudaMemsetAsync(ticket, 0, 4, S.stream));
+  k_reduce<Op><<<grid, RBLOCK, 0, S.stream>>>(in, n, partial, ticket, result_dev, count_flags ? 1 : 0);
+  launch_check("k_reduce");
+}
+template <class T> int reduce_units(int n) {
+  (void)n;
+  return (256 + (st().sm_count > 0 ? st().sm_count : 152) * 2 * 8 + 7) / 8 + 64;
+}
+
+template <class Op>
+typename Op::T reduce_to_host(vec_p s, int n, vec_p scratch, bool count_flags = false) {
+  typedef typename Op::T T;
+  ensure_init();
+  State &S = st();
+  if (!S.ready) return Op::init();
+  T *res = (T *)((char *)S.d_small + 64);
+  run_reduce<Op>((const T *)s, n, res, scratch, count_flags);
+  T v = Op::init();
+  GCVL_CK(cudaMemcpyAsync(S.h_small, res, sizeof(T), cudaMemcpyDeviceToHost, S.stream));
+  GCVL_CK(cudaStreamSynchronize(S.stream));
+  memcpy(&v, S.h_small, sizeof(T));
+  return v;
+}
+
+template <class Op>
+void seg_reduce(vec_p d, vec_p s, vec_p sd, int n, int m, vec_p scratch, bool count_flags,
+                const char *name) {
+  typedef typename Op::T T;
+  ensure_init();
+  if (m <= 0) return;
+  if (m == 1) {  // vprims.c:170: a single segment reduces to the unsegmented result
+    run_reduce<Op>((const T *)s, n, (T *)d, scratch, count_flags);
+    return;
+  }
+  if (n <= 0) {
+    k_fill<Op><<<ceil_div(m, 256), 256, 0, stream()>>>((T *)d, m);
+    launch_check(name);
+    return;
+  }
+  run_scan<Op, M_REDUCE, true>((T *)d, (const T *)s, nullptr, sd, n, m, scratch, count_flags, name);
+}
+
+template <class Op>
+void seg_scan(vec_p d, vec_p s, vec_p sd, int n, int m, vec_p scratch, const char *name) {
+  typedef typename Op::T T;
+  if (m == 1 || sd == nullptr)
+    run_scan<Op, M_SCAN, false>((T *)d, (const T *)s, nullptr, nullptr, n, 1, scratch, false, name);
+  else
+    run_scan<Op, M_SCAN, true>((T *)d, (const T *)s, nullptr, sd, n, m, scratch, false, name);
+}
+
+// ---------------------------------------------------------- segdes build ---
+__global__ void k_granules(SegView sv, int *gran, int ng) {
+  int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g > ng) return;
+  if (g == ng) { gran[g] = sv.m; return; }
+  int k = g * kGranule;  // < n
+  int lo = 0, hi = sv.m - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (__ldg(sv.off + mid) <= k) lo = mid; else hi = mid - 1;
+  }
+  gran[g] = lo;
+}
+
+void make_segdes(vec_p sd, vec_p l, int n, int m, vec_p scratch) {
+  ensure_init();
+  State &S = st();
+  int *base = (int *)sd;
+  int *len = base;
+  int *off = base + segdes_off_words(m);
+  int *gran = base + segdes_gran_words(m);
+  if (m <= 0) {
+    GCVL_CK(cudaMemsetAsync(off, 0, 4, S.stream));
+  } else if ((const int *)l == len) {
+    // lengths already in place: scan them into the offsets only
+    run_scan<AddZ, M_SCAN, false>(off, len, nullptr, nullptr, m, 1, scratch, false, "mke_fov");
+    GCVL_CK(cudaMemcpyAsync(off + m, &n, 4, cudaMemcpyHostToDevice, S.stream));
+  } else {
+    run_scan<AddZ, M_OFFSETS, false>(off, (const int *)l, len, nullptr, m, 1, scratch, false, "mke_fov");
+  }
+  int ng = (n + kGranule - 1) / kGranule;
+  SegView sv = seg_view(sd, n, m);
+  if (m <= 0) ng = 0;
+  k_granules<<<ceil_div(ng + 1, 256), 256, 0, S.stream>>>(sv, gran, ng);
+  launch_check("k_granules");
+}
+
+}  // namespace gcvl
+
+using namespace gcvl;
+
+// ============================================================ C ABI exports
+#define SCAN_EXPORTS(NAME, L, OP, T)                                                        \
+  GCVL_EXPORT void NAME##_su##L(vec_p d, vec_p s, int len, vec_p scratch) {                 \
+    run_scan<OP, M_SCAN, false>((T *)d, (const T *)s, nullptr, nullptr, len, 1, scratch,     \
+                                false, #NAME "_su" #L);                                      \
+  }                                                                                          \
+  GCVL_EXPORT int NAME##_su##L##_scratch(int len) { return scan_units<T>(len); }             \
+  GCVL_EXPORT unsigned NAME##_su##L##_inplace(void) { return INPLACE_1; }                    \
+  GCVL_EXPORT void NAME##_se##L(vec_p d, vec_p s, vec_p sd, int n, int m, vec_p scratch) {   \
+    seg_scan<OP>(d, s, sd, n, m, scratch, #NAME "_se" #L);                                   \
+  }                                                                                          \
+  GCVL_EXPORT int NAME##_se##L##_scratch(int n, int m) { (void)m; return scan_units<T>(n); } \
+  GCVL_EXPORT unsigned NAME##_se##L##_inplace(void) { return INPLACE_1; }                    \
+  GCVL_EXPORT T NAME##_ru##L(vec_p s, int len, vec_p scratch) {                              \
+    return reduce_to_host<OP>(s, len, scratch);                                              \
+  }                                                                                          \
+  GCVL_EXPORT int NAME##_ru##L##_scratch(int len) { return reduce_units<T>(len); }           \
+  GCVL_EXPORT unsigned NAME##_ru##L##_inplace(void) { return INPLACE_NONE; }                 \
+  GCVL_EXPORT void NAME##_re##L(vec_p d, vec_p s, vec_p sd, int n, int m, vec_p scratch) {   \
+    seg_reduce<OP>(d, s, sd, n, m, scratch, false, #NAME "_re" #L);                          \
+  }                                                                                          \
+  GCVL_EXPORT int NAME##_re##L##_scratch(int n, int m) {                                     \
+    (void)m; int a = scan_units<T>(n), b = reduce_units<T>(n); return a > b ? a : b;         \
+  }                                                                                          \
+  GCVL_EXPORT unsigned NAME##_re##L##_inplace(void) { return INPLACE_NONE; }
+
+SCAN_EXPORTS(add, z, AddZ, int)
+SCAN_EXPORTS(add, d, AddD, double)
+SCAN_EXPORTS(mul, z, MulZ, int)
+SCAN_EXPORTS(mul, d, MulD, double)
+SCAN_EXPORTS(min, z, MinZ, int)
+SCAN_EXPORTS(min, d, MinD, double)
+SCAN_EXPORTS(max, z, MaxZ, int)
+SCAN_EXPORTS(max, d, MaxD, double)
+SCAN_EXPORTS(and, b, AndB, cvl_bool)
+SCAN_EXPORTS(and, z, AndZ, int)
+SCAN_EXPORTS(ior, b, IorB, cvl_bool)
+SCAN_EXPORTS(ior, z, IorZ, int)
+SCAN_EXPORTS(xor, b, XorB, cvl_bool)
+SCAN_EXPORTS(xor, z, XorZ, int)
+
+// Segment descriptors (facilt.c:112-144).
+GCVL_EXPORT void mke_fov(vec_p sd, vec_p l, int n, int m, vec_p scratch) {
+  make_segdes(sd, l, n, m, scratch);
+}
+GCVL_EXPORT unsigned mke_fov_inplace(void) { return INPLACE_NONE; }
+GCVL_EXPORT int mke_fov_scratch(int n, int m) { (void)n; return scan_units<int>(m); }
+GCVL_EXPORT void len_fos(vec_p l, vec_p sd, int n, int m, vec_p scratch) {
+  (void)n; (void)scratch;
+  ensure_init();
+  if (m <= 0 || l == sd) return;
+  GCVL_CK(cudaMemcpyAsync(l, sd, (size_t)m * 4, cudaMemcpyDeviceToDevice, stream()));
+}
+GCVL_EXPORT int len_fos_scratch(int n, int m) { (void)n; (void)m; return 0; }
+GCVL_EXPORT unsigned len_fos_inplace(void) { return INPLACE_NONE; }
+
+// Pack, phase 1 (library.c:55-133): count true flags.
+GCVL_EXPORT int pk1_luv(vec_p f, int len, vec_p scratch) {
+  return reduce_to_host<CountB>(f, len, scratch, true);
+}
+GCVL_EXPORT int pk1_luv_scratch(int len) { return reduce_units<int>(len); }
+GCVL_EXPORT unsigned pk1_luv_inplace(void) { return INPLACE_NONE; }
+GCVL_EXPORT void pk1_lev(vec_p ds, vec_p f, vec_p sd, int n, int m, vec_p scratch) {
+  seg_reduce<CountB>(ds, f, sd, n, m, scratch, true, "pk1_lev");
+}
+GCVL_EXPORT int pk1_lev_scratch(int n, int m) {
+  (void)m; int a = scan_units<int>(n), b = reduce_units<int>(n); return a > b ? a : b;
+}
+GCVL_EXPORT unsigned pk1_lev_inplace(void) { return INPLACE_NONE; }

@@ -1,0 +1,444 @@
+// vprims.cu -- extract / replace / distribute / index (segmented forms),
+// permute / back-permute, the flag and default permutes, and pack.
+//
+// Semantics: nesl/cvl/serial/vprims.c:207-467, vecops.c:22-286 and
+// library.c:12-165.  Segmented forms find each element's segment from the
+// device segment descriptor (offsets + granule table) instead of storing a
+// per-element segment id, so a call reads only its own operands.
+//
+// Permutes with repeated indices: NESL's permute takes a permutation.  When
+// an index repeats, which value lands at the collided position is
+// unspecified here (the serial CVL keeps the last writer).
+#include "gcvl.cuh"
+
+namespace gcvl {
+
+constexpr int VBLOCK = 256;
+constexpr int SITEMS = 4;  // consecutive elements per thread in segmented maps
+
+inline int grid_for(long work, int per_block) {
+  long g = (work + per_block - 1) / per_block;
+  return (int)(g < 1 ? 1 : g);
+}
+
+// Calls f(k, s, seg_start) for every element k of a segmented vector, with s
+// the segment holding k.  Each thread walks SITEMS consecutive elements.
+template <class F>
+__global__ void __launch_bounds__(VBLOCK) k_segwalk(F f, SegView sv) {
+  long k0 = ((long)blockIdx.x * VBLOCK + threadIdx.x) * SITEMS;
+  if (k0 >= sv.n) return;
+  int cnt = (int)min((long)SITEMS, (long)sv.n - k0);
+  int s = seg_of(sv, (int)k0);
+  int start = __ldg(sv.off + s), end = __ldg(sv.off + s + 1);
+  for (int i = 0; i < cnt; i++) {
+    int k = (int)k0 + i;
+    while (k >= end) { ++s; start = end; end = __ldg(sv.off + s + 1); }
+    f(k, s, start);
+  }
+}
+template <class F> void segwalk(F f, const SegView &sv, const char *name) {
+  if (sv.n <= 0 || sv.m <= 0) return;
+  k_segwalk<F><<<grid_for(((long)sv.n + SITEMS - 1) / SITEMS, VBLOCK), VBLOCK, 0, stream()>>>(f, sv);
+  launch_check(name);
+}
+// f(i) for i in [0, n)
+template <class F> __global__ void __launch_bounds__(VBLOCK) k_each(F f, long n) {
+  const long stride = (long)gridDim.x * VBLOCK;
+  for (long i = (long)blockIdx.x * VBLOCK + threadIdx.x; i < n; i += stride) f(i);
+}
+template <class F> void each(F f, long n, const char *name) {
+  if (n <= 0) return;
+  long g = (n + VBLOCK - 1) / VBLOCK, cap = (long)st().sm_count * 32;
+  k_each<F><<<(int)(g < cap ? g : cap), VBLOCK, 0, stream()>>>(f, n);
+  launch_check(name);
+}
+
+// ----------------------------------------------------------- functors ---
+template <class T> struct ExtSeg {  // d[g] = s[off[g] + i[g]]
+  T *d; const T *s; const int *i; const int *off;
+  __device__ void operator()(long g) const { d[g] = s[(long)off[g] + i[g]]; }
+};
+template <class T> struct RepSeg {  // d[off[g] + i[g]] = v[g]
+  T *d; const int *i; const T *v; const int *off;
+  __device__ void operator()(long g) const { d[(long)off[g] + i[g]] = v[g]; }
+};
+template <class T> struct DisSeg {  // d[k] = v[seg(k)]
+  T *d; const T *v;
+  __device__ void operator()(int k, int s, int) const { d[k] = __ldg(v + s); }
+};
+struct IndSeg {  // d[k] = init[s] + stride[s] * (k - start)
+  int *d; const int *init; const int *stride;
+  __device__ void operator()(int k, int s, int start) const {
+    d[k] = (int)((unsigned)__ldg(init + s) + (unsigned)__ldg(stride + s) * (unsigned)(k - start));
+  }
+};
+template <class T> struct Perm {  // d[i[k]] = s[k]
+  T *d; const T *s; const int *i;
+  __device__ void operator()(long k) const { d[__ldg(i + k)] = __ldcs(s + k); }
+};
+template <class T> struct PermSeg {  // d[start + i[k]] = s[k]
+  T *d; const T *s; const int *i;
+  __device__ void operator()(int k, int, int start) const { d[(long)start + __ldg(i + k)] = __ldcs(s + k); }
+};
+template <class T> struct BPerm {  // d[k] = s[i[k]]
+  T *d; const T *s; const int *i;
+  __device__ void operator()(long k) const { d[k] = __ldg(s + __ldg(i + k)); }
+};
+template <class T> struct BPermSeg {  // d[k] = s[off_s[seg_d(k)] + i[k]]
+  T *d; const T *s; const int *i; const int *off_s;
+  __device__ void operator()(int k, int sg, int) const {
+    d[k] = __ldg(s + (long)__ldg(off_s + sg) + __ldg(i + k));
+  }
+};
+template <class T> struct FPerm {  // if f[k]: d[i[k]] = s[k]
+  T *d; const T *s; const int *i; const int *f;
+  __device__ void operator()(long k) const { if (__ldg(f + k)) d[__ldg(i + k)] = __ldcs(s + k); }
+};
+template <class T> struct FPermSeg {  // if f[k]: d[off_d[seg_s(k)] + i[k]] = s[k]
+  T *d; const T *s; const int *i; const int *f; const int *off_d;
+  __device__ void operator()(int k, int sg, int) const {
+    if (f == nullptr || __ldg(f + k)) d[(long)__ldg(off_d + sg) + __ldg(i + k)] = __ldcs(s + k);
+  }
+};
+template <class T> struct BFPerm {  // d[k] = f[k] ? s[i[k]] : 0
+  T *d; const T *s; const int *i; const int *f;
+  __device__ void operator()(long k) const { d[k] = __ldg(f + k) ? __ldg(s + __ldg(i + k)) : (T)0; }
+};
+template <class T> struct BFPermSeg {  // d[k] = f[k] ? s[off_s[seg_d(k)] + i[k]] : 0
+  T *d; const T *s; const int *i; const int *f; const int *off_s; int m_s;
+  __device__ void operator()(int k, int sg, int) const {
+    T v = (T)0;
+    if (sg < m_s && __ldg(f + k)) v = __ldg(s + (long)__ldg(off_s + sg) + __ldg(i + k));
+    d[k] = v;
+  }
+};
+
+template <class T> void copy_dev(vec_p d, vec_p s, int n) {
+  if (n <= 0 || d == s) return;
+  GCVL_CK(cudaMemcpyAsync(d, s, (size_t)n * sizeof(T), cudaMemcpyDeviceToDevice, stream()));
+}
+
+// ---------------------------------------------------------------- pack ---
+// Stable compaction in one pass: a CTA counts the true flags of its tile,
+// gets the number of true flags in earlier tiles by decoupled look-back,
+// compacts its kept values in shared memory and writes them as one
+// contiguous, coalesced run.
+constexpr int PBLOCK = 256, PITEMS = 16, PTILE = PBLOCK * PITEMS;
+
+template <class T>
+__global__ void __launch_bounds__(PBLOCK) k_pack(T *__restrict__ d, const T *__restrict__ s,
+                                                const int *__restrict__ f, int n, LookbackMem lb,
+                                                unsigned *status, int spin_limit) {
+  constexpr int PE = 32;  // padding period of the int staging buffer
+  __shared__ int s_rank[PTILE + PTILE / PE];
+  __shared__ T s_val[PTILE];
+  __shared__ int s_wsum[PBLOCK / 32];
+  __shared__ int s_prefix, s_count;
+  __shared__ unsigned s_tile;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (tid == 0) s_tile = atomicAdd(lb.counter, 1u);
+  __syncthreads();
+  const int tile = (int)s_tile;
+  const long base = (long)tile * PTILE;
+  const int valid = (int)min((long)PTILE, (long)n - base);
+
+  // flags: coalesced striped loads, transposed to 16 consecutive per thread
+  const int wbase = warp * 32 * PITEMS;
+#pragma unroll
+  for (int j = 0; j < PITEMS; j++) {
+    int e = wbase + j * 32 + lane;
+    s_rank[e + e / PE] = (e < valid) ? (__ldcs(f + base + e) != 0) : 0;
+  }
+  __syncwarp();
+  unsigned bits = 0;
+#pragma unroll
+  for (int i = 0; i < PITEMS; i++) {
+    int e = tid * PITEMS + i;
+    bits |= (unsigned)s_rank[e + e / PE] << i;
+  }
+  // exclusive scan of the per-thread counts across the CTA
+  int c = __popc(bits), incl = c;
+#pragma unroll
+  for (int dd = 1; dd < 32; dd <<= 1) {
+    int o = shfl_up(incl, dd);
+    if (lane >= dd) incl += o;
+  }
+  if (lane == 31) s_wsum[warp] = incl;
+  __syncthreads();
+  int wpre = 0, total = 0;
+#pragma unroll
+  for (int w = 0; w < PBLOCK / 32; w++) {
+    int v = s_wsum[w];
+    if (w < warp) wpre += v;
+    total += v;
+  }
+  int r = wpre + incl - c;
+  // rank of every element within the tile's output (-1 when dropped)
+#pragma unroll
+  for (int i = 0; i < PITEMS; i++) {
+    int e = tid * PITEMS + i;
+    s_rank[e + e / PE] = ((bits >> i) & 1u) ? r++ : -1;
+  }
+
+  // decoupled look-back over tile counts (int add, no segments)
+  if (warp == 0) {
+    if (lane == 0) {
+      if (tile == 0) { st_relaxed(lb.inc + tile, (unsigned long long)total); st_release(lb.flags + tile, TS_INC); }
+      else { st_relaxed(lb.agg + tile, (unsigned long long)total); st_release(lb.flags + tile, TS_AGG); }
+    }
+    long P = 0;
+    if (tile > 0) {
+      int pred = tile - 1;
+      while (true) {
+        int t = pred - lane;
+        unsigned fl = TS_INC;
+        long val = 0;
+        if (t >= 0) {
+          int it = 0;
+          fl = ld_acquire(lb.flags + t);
+          while (fl == TS_EMPTY) {
+            if (++it >= spin_limit) break;
+            __nanosleep(32);
+            fl = ld_acquire(lb.flags + t);
+          }
+          if (fl == TS_EMPTY) { atomicOr(status, DEV_TIMEOUT); fl = TS_INC; }
+          else val = (long)ld_relaxed(fl == TS_INC ? lb.inc + t : lb.agg + t);
+        }
+        unsigned incm = __ballot_sync(0xffffffffu, fl == TS_INC);
+        int stop = incm ? __ffs(incm) - 1 : 31;
+        if (lane > stop) val = 0;
+#pragma unroll
+        for (int dd = 16; dd > 0; dd >>= 1) val += shfl_down(val, dd);
+        P += shfl_idx(val, 0);
+        if (incm) break;
+        pred -= 32;
+      }
+      if (lane == 0) {
+        st_relaxed(lb.inc + tile, (unsigned long long)(P + total));
+        st_release(lb.flags + tile, TS_INC);
+      }
+    }
+    if (lane == 0) { s_prefix = (int)P; s_count = total; }
+  }
+  __syncthreads();
+  // values: coalesced striped loads, placed at their rank in shared memory
+#pragma unroll
+  for (int j = 0; j < PITEMS; j++) {
+    int e = j * PBLOCK + tid;
+    int rk = s_rank[e + e / PE];
+    if (rk >= 0) s_val[rk] = __ldcs(s + base + e);
+  }
+  __syncthreads();
+  const long out0 = s_prefix;
+  const int cnt = s_count;
+  for (int e = tid; e < cnt; e += PBLOCK) d[out0 + e] = s_val[e];
+}
+
+template <class T> void pack(vec_p d, vec_p s, vec_p f, int n, vec_p scratch, const char *name) {
+  ensure_init();
+  State &S = st();
+  if (n <= 0) return;
+  int tiles = ceil_div(n, PTILE);
+  void *mem = scratch_or_work(scratch, lookback_bytes(tiles));
+  if (!mem) return;
+  LookbackMem lb = lookback_carve(mem, tiles);
+  GCVL_CK(cudaMemsetAsync(mem, 0, lookback_clear_bytes(tiles), S.stream));
+  k_pack<T><<<tiles, PBLOCK, 0, S.stream>>>((T *)d, (const T *)s, (const int *)f, n, lb, S.d_status,
+                                            S.spin_limit);
+  launch_check(name);
+}
+int pack_units(int n) { return n <= 0 ? 0 : lookback_units(ceil_div(n, PTILE)); }
+
+}  // namespace gcvl
+
+using namespace gcvl;
+
+#define META1(NAME, INPL)                                                     \
+  GCVL_EXPORT int NAME##_scratch(int len) { (void)len; return 0; }           \
+  GCVL_EXPORT unsigned NAME##_inplace(void) { return INPL; }
+#define META_SEG(NAME, INPL)                                                  \
+  GCVL_EXPORT int NAME##_scratch(int n, int m) { (void)n; (void)m; return 0; } \
+  GCVL_EXPORT unsigned NAME##_inplace(void) { return INPL; }
+#define META2(NAME, INPL)                                                     \
+  GCVL_EXPORT int NAME##_scratch(int a, int b) { (void)a; (void)b; return 0; } \
+  GCVL_EXPORT unsigned NAME##_inplace(void) { return INPL; }
+#define META_SEG2(NAME, INPL)                                                 \
+  GCVL_EXPORT int NAME##_scratch(int a, int b, int c, int e) {                \
+    (void)a; (void)b; (void)c; (void)e; return 0; }                          \
+  GCVL_EXPORT unsigned NAME##_inplace(void) { return INPL; }
+
+// ------------------------------------------------ extract / replace ---
+// ext_vu* / rep_vu* move one element (vprims.c:207-262); extract returns to
+// the host, so it synchronises.
+#define EXT_REP(L, T)                                                                  \
+  GCVL_EXPORT T ext_vu##L(vec_p v, int i, int len, vec_p scratch) {                    \
+    (void)len; (void)scratch; ensure_init();                                          \
+    T out = (T)0;                                                                      \
+    GCVL_CK(cudaMemcpyAsync(st().h_small, (T *)v + i, sizeof(T), cudaMemcpyDeviceToHost, \
+                            stream()));                                                \
+    GCVL_CK(cudaStreamSynchronize(stream()));                                          \
+    memcpy(&out, st().h_small, sizeof(T));                                             \
+    return out;                                                                        \
+  }                                                                                    \
+  META1(ext_vu##L, INPLACE_NONE)                                                       \
+  GCVL_EXPORT void ext_ve##L(vec_p d, vec_p s, vec_p i, vec_p sd, int n, int m,        \
+                             vec_p scratch) {                                          \
+    (void)scratch; ensure_init();                                                     \
+    SegView sv = seg_view(sd, n, m);                                                   \
+    each(ExtSeg<T>{(T *)d, (const T *)s, (const int *)i, sv.off}, m, "ext_ve" #L);     \
+  }                                                                                    \
+  META_SEG(ext_ve##L, INPLACE_2)                                                       \
+  GCVL_EXPORT void rep_ve##L(vec_p d, vec_p s, vec_p v, vec_p sd, int n, int m,        \
+                             vec_p scratch) {                                          \
+    (void)scratch; ensure_init();                                                     \
+    SegView sv = seg_view(sd, n, m);                                                   \
+    each(RepSeg<T>{(T *)d, (const int *)s, (const T *)v, sv.off}, m, "rep_ve" #L);     \
+  }                                                                                    \
+  META_SEG(rep_ve##L, INPLACE_NONE)                                                    \
+  GCVL_EXPORT void dis_ve##L(vec_p d, vec_p v, vec_p sd, int n, int m, vec_p scratch) { \
+    (void)scratch; ensure_init();                                                     \
+    segwalk(DisSeg<T>{(T *)d, (const T *)v}, seg_view(sd, n, m), "dis_ve" #L);        \
+  }                                                                                    \
+  META_SEG(dis_ve##L, INPLACE_NONE)
+EXT_REP(z, int)
+EXT_REP(b, cvl_bool)
+EXT_REP(d, double)
+
+// Replace writes one element from the host value (vprims.c:236-262).
+GCVL_EXPORT void rep_vuz(vec_p v, int i, int val, int len, vec_p scratch) {
+  (void)len; (void)scratch; ensure_init();
+  GCVL_CK(cudaMemcpyAsync((int *)v + i, &val, 4, cudaMemcpyHostToDevice, stream()));
+  GCVL_CK(cudaStreamSynchronize(stream()));
+}
+META1(rep_vuz, INPLACE_NONE)
+GCVL_EXPORT void rep_vub(vec_p v, int i, cvl_bool val, int len, vec_p scratch) {
+  (void)len; (void)scratch; ensure_init();
+  int b = val != 0;
+  GCVL_CK(cudaMemcpyAsync((int *)v + i, &b, 4, cudaMemcpyHostToDevice, stream()));
+  GCVL_CK(cudaStreamSynchronize(stream()));
+}
+META1(rep_vub, INPLACE_NONE)
+GCVL_EXPORT void rep_vud(vec_p v, int i, double val, int len, vec_p scratch) {
+  (void)len; (void)scratch; ensure_init();
+  GCVL_CK(cudaMemcpyAsync((double *)v + i, &val, 8, cudaMemcpyHostToDevice, stream()));
+  GCVL_CK(cudaStreamSynchronize(stream()));
+}
+META1(rep_vud, INPLACE_NONE)
+
+// Segmented index (library.c:28-49).
+GCVL_EXPORT void ind_lez(vec_p d, vec_p init, vec_p stride, vec_p sd, int n, int m, vec_p scratch) {
+  (void)scratch; ensure_init();
+  segwalk(IndSeg{(int *)d, (const int *)init, (const int *)stride}, seg_view(sd, n, m), "ind_lez");
+}
+META_SEG(ind_lez, INPLACE_NONE)
+
+// ------------------------------------------------------------- permutes ---
+#define PERMS(L, T)                                                                     \
+  GCVL_EXPORT void smp_pu##L(vec_p d, vec_p s, vec_p i, int len, vec_p scratch) {       \
+    (void)scratch; ensure_init();                                                       \
+    each(Perm<T>{(T *)d, (const T *)s, (const int *)i}, len, "smp_pu" #L);              \
+  }                                                                                     \
+  META1(smp_pu##L, INPLACE_NONE)                                                        \
+  GCVL_EXPORT void smp_pe##L(vec_p d, vec_p s, vec_p i, vec_p sd, int n, int m,         \
+                             vec_p scratch) {                                           \
+    (void)scratch; ensure_init();                                                       \
+    if (m == 1) { each(Perm<T>{(T *)d, (const T *)s, (const int *)i}, n, "smp_pe" #L); return; } \
+    segwalk(PermSeg<T>{(T *)d, (const T *)s, (const int *)i}, seg_view(sd, n, m), "smp_pe" #L); \
+  }                                                                                     \
+  META_SEG(smp_pe##L, INPLACE_NONE)                                                     \
+  GCVL_EXPORT void bck_pu##L(vec_p d, vec_p s, vec_p i, int s_len, int d_len,           \
+                             vec_p scratch) {                                           \
+    (void)s_len; (void)scratch; ensure_init();                                          \
+    each(BPerm<T>{(T *)d, (const T *)s, (const int *)i}, d_len, "bck_pu" #L);           \
+  }                                                                                     \
+  META2(bck_pu##L, INPLACE_2)                                                           \
+  GCVL_EXPORT void bck_pe##L(vec_p d, vec_p s, vec_p i, vec_p sd_s, int n_s, int m_s,   \
+                             vec_p sd_d, int n_d, int m_d, vec_p scratch) {             \
+    (void)scratch; ensure_init();                                                       \
+    if (m_s == 1) { each(BPerm<T>{(T *)d, (const T *)s, (const int *)i}, n_d, "bck_pe" #L); return; } \
+    SegView ss = seg_view(sd_s, n_s, m_s);                                              \
+    segwalk(BPermSeg<T>{(T *)d, (const T *)s, (const int *)i, ss.off},                 \
+            seg_view(sd_d, n_d, m_d), "bck_pe" #L);                                     \
+  }                                                                                     \
+  META_SEG2(bck_pe##L, INPLACE_2)                                                       \
+  GCVL_EXPORT void fpm_pu##L(vec_p d, vec_p s, vec_p i, vec_p f, int len_src,           \
+                             int len_dest, vec_p scratch) {                             \
+    (void)len_dest; (void)scratch; ensure_init();                                       \
+    each(FPerm<T>{(T *)d, (const T *)s, (const int *)i, (const int *)f}, len_src, "fpm_pu" #L); \
+  }                                                                                     \
+  META2(fpm_pu##L, INPLACE_NONE)                                                        \
+  GCVL_EXPORT void fpm_pe##L(vec_p d, vec_p s, vec_p i, vec_p f, vec_p sd_s, int n_s,   \
+                             int m_s, vec_p sd_d, int n_d, int m_d, vec_p scratch) {    \
+    (void)scratch; ensure_init();                                                       \
+    if (m_s == 1) { fpm_pu##L(d, s, i, f, n_s, n_d, scratch); return; }                 \
+    SegView sdd = seg_view(sd_d, n_d, m_d);                                             \
+    segwalk(FPermSeg<T>{(T *)d, (const T *)s, (const int *)i, (const int *)f, sdd.off}, \
+            seg_view(sd_s, n_s, m_s), "fpm_pe" #L);                                     \
+  }                                                                                     \
+  META_SEG2(fpm_pe##L, INPLACE_NONE)                                                    \
+  GCVL_EXPORT void bfp_pu##L(vec_p d, vec_p s, vec_p i, vec_p f, int len_src,           \
+                             int len_dest, vec_p scratch) {                             \
+    (void)len_src; (void)scratch; ensure_init();                                        \
+    each(BFPerm<T>{(T *)d, (const T *)s, (const int *)i, (const int *)f}, len_dest, "bfp_pu" #L); \
+  }                                                                                     \
+  META2(bfp_pu##L, INPLACE_NONE)                                                        \
+  GCVL_EXPORT void bfp_pe##L(vec_p d, vec_p s, vec_p i, vec_p f, vec_p sd_s, int n_s,   \
+                             int m_s, vec_p sd_d, int n_d, int m_d, vec_p scratch) {    \
+    (void)scratch; ensure_init();                                                       \
+    if (m_s == 1) { bfp_pu##L(d, s, i, f, n_s, n_d, scratch); return; }                 \
+    SegView ss = seg_view(sd_s, n_s, m_s);                                              \
+    segwalk(BFPermSeg<T>{(T *)d, (const T *)s, (const int *)i, (const int *)f, ss.off, m_s}, \
+            seg_view(sd_d, n_d, m_d), "bfp_pe" #L);                                     \
+  }                                                                                     \
+  META_SEG2(bfp_pe##L, INPLACE_NONE)                                                    \
+  GCVL_EXPORT void dpe_pu##L(vec_p d, vec_p s, vec_p i, vec_p v, int len_src,           \
+                             int len_dest, vec_p scratch) {                             \
+    ensure_init();                                                                      \
+    copy_dev<T>(d, v, len_dest);                                                        \
+    smp_pu##L(d, s, i, len_src, scratch);                                               \
+  }                                                                                     \
+  META2(dpe_pu##L, INPLACE_3)                                                           \
+  GCVL_EXPORT void dpe_pe##L(vec_p d, vec_p s, vec_p i, vec_p v, vec_p sd_s, int n_s,   \
+                             int m_s, vec_p sd_d, int n_d, int m_d, vec_p scratch) {    \
+    ensure_init();                                                                      \
+    if (m_s == 1) { dpe_pu##L(d, s, i, v, n_s, n_d, scratch); return; }                 \
+    copy_dev<T>(d, v, n_d);                                                             \
+    SegView sdd = seg_view(sd_d, n_d, m_d);                                             \
+    segwalk(FPermSeg<T>{(T *)d, (const T *)s, (const int *)i, nullptr, sdd.off},        \
+            seg_view(sd_s, n_s, m_s), "dpe_pe" #L);                                     \
+  }                                                                                     \
+  META_SEG2(dpe_pe##L, INPLACE_3)                                                       \
+  GCVL_EXPORT void dfp_pu##L(vec_p d, vec_p s, vec_p i, vec_p f, vec_p v, int len_src,  \
+                             int len_dest, vec_p scratch) {                             \
+    ensure_init();                                                                      \
+    copy_dev<T>(d, v, len_dest);                                                        \
+    fpm_pu##L(d, s, i, f, len_src, len_dest, scratch);                                  \
+  }                                                                                     \
+  META2(dfp_pu##L, INPLACE_4)                                                           \
+  GCVL_EXPORT void dfp_pe##L(vec_p d, vec_p s, vec_p i, vec_p f, vec_p v, vec_p sd_s,   \
+                             int n_s, int m_s, vec_p sd_d, int n_d, int m_d,            \
+                             vec_p scratch) {                                           \
+    ensure_init();                                                                      \
+    copy_dev<T>(d, v, n_d);                                                             \
+    if (m_s == 1) fpm_pu##L(d, s, i, f, n_s, n_d, scratch);                             \
+    else fpm_pe##L(d, s, i, f, sd_s, n_s, m_s, sd_d, n_d, m_d, scratch);                \
+  }                                                                                     \
+  META_SEG2(dfp_pe##L, INPLACE_4)                                                       \
+  GCVL_EXPORT void pk2_lu##L(vec_p d, vec_p s, vec_p f, int src_len, int dest_len,      \
+                             vec_p scratch) {                                           \
+    (void)dest_len; pack<T>(d, s, f, src_len, scratch, "pk2_lu" #L);                    \
+  }                                                                                     \
+  GCVL_EXPORT int pk2_lu##L##_scratch(int len) { return pack_units(len); }              \
+  GCVL_EXPORT unsigned pk2_lu##L##_inplace(void) { return INPLACE_NONE; }               \
+  GCVL_EXPORT void pk2_le##L(vec_p d, vec_p s, vec_p f, vec_p sd_s, int n_s, int m_s,   \
+                             vec_p sd_d, int n_d, int m_d, vec_p scratch) {             \
+    (void)sd_s; (void)m_s; (void)sd_d; (void)n_d; (void)m_d;                            \
+    pack<T>(d, s, f, n_s, scratch, "pk2_le" #L);                                        \
+  }                                                                                     \
+  GCVL_EXPORT int pk2_le##L##_scratch(int a, int b, int c, int e) {                     \
+    (void)b; (void)c; (void)e; return pack_units(a);                                    \
+  }                                                                                     \
+  GCVL_EXPORT unsigned pk2_le##L##_inplace(void) { return INPLACE_NONE; }
+PERMS(z, int)
+PERMS(b, cvl_bool)
+PERMS(d, double)

@@ -1,0 +1,50 @@
+"""The C ABI: the library loads without a GPU and exports every function
+include/cvl_gb300.h declares, which are exactly the prototypes of the
+reference's cvl.h plus the gcvl_* extensions."""
+import re
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def _declared():
+    names = set()
+    for h in (ROOT / "include").glob("*.h"):
+        txt = h.read_text()
+        txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+        for m in re.finditer(r"^\s*(?:[A-Za-z_][\w ]*?[\s\*]+)(\w+)\s*\([^;{]*\)\s*;", txt, re.M):
+            names.add(m.group(1))
+    return names
+
+
+def test_header_matches_reference_abi():
+    from neslgpu_gb300 import abi
+    declared = _declared()
+    missing = set(abi.CVL) - declared
+    assert not missing, f"cvl.h functions not declared: {sorted(missing)[:20]}"
+    assert set(abi.EXTENSIONS) <= declared
+
+
+def test_library_exports_every_declared_symbol():
+    import ctypes
+    from neslgpu_gb300.cvl import LIB_PATH
+    assert LIB_PATH.exists(), "build the library first"
+    lib = ctypes.CDLL(str(LIB_PATH))
+    missing = [n for n in sorted(_declared()) if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_host_side_functions_without_gpu():
+    """Size, scratch, in-place and pointer arithmetic need no device."""
+    from neslgpu_gb300.cvl import load
+    c = load()
+    assert c.siz_foz(3) == 2 and c.siz_fob(3) == 2 and c.siz_fod(3) == 3
+    assert c.siz_fos(100, 10) >= c.siz_foz(10)
+    assert c.add_fov(1000, 3) == 1024 and c.sub_fov(1024, 1000) == 3
+    assert c.cmp_fov(1000, 1024) == -3 and c.eql_fov(8, 8) == 1
+    assert c.add_sez_scratch(1 << 20, 100) > 0
+    assert c.add_sez_inplace() == 1
+    assert c.rku_luz_scratch(1 << 20) > 0 and c.rku_lez_scratch(1 << 20, 5) > c.rku_luz_scratch(1 << 20)
+    assert c.mke_fov_inplace() == 0

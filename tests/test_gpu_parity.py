@@ -1,0 +1,41 @@
+"""libcvl_gb300.so against the oracle, primitive by primitive, through the
+C ABI.  Integer, boolean and index results must be bit-identical; float64
+sums agree within |a - b| <= 1e-12 * max(|b|, S) (S = sum of |x| over the
+same prefix or segment), float64 products within 1e-12 relative, and CUDA
+transcendentals within 1e-13 relative of libm."""
+import numpy as np
+import pytest
+
+from cases import compare, make_cases
+
+pytestmark = pytest.mark.gpu
+
+SIZES = [0, 1, 7, 4097, 100_003]
+KINDS = ["geo", "tiny", "empty", "bimodal", "one", "long"]
+
+
+def _run_all(gpu, oracle, n, kind, seed):
+    failures = []
+    for cid, fn, cmp, ctx in make_cases(n=n, seed=seed, lengths_kind=kind):
+        want = fn(oracle)
+        try:
+            got = fn(gpu)
+            compare(cmp, got, want, ctx)
+        except Exception as e:  # collect every mismatch of the sweep
+            failures.append(f"{cid}: {e}")
+    assert not failures, f"n={n} kind={kind}:\n" + "\n".join(failures[:40])
+
+
+@pytest.mark.parametrize("n", SIZES)
+def test_parity_sizes(gpu, oracle, n):
+    _run_all(gpu, oracle, n, "geo", seed=100 + n)
+
+
+@pytest.mark.parametrize("kind", KINDS)
+def test_parity_segment_shapes(gpu, oracle, kind):
+    _run_all(gpu, oracle, 60_001, kind, seed=5)
+
+
+def test_parity_large(gpu, oracle):
+    # several tiles per segment and several segments per tile at once
+    _run_all(gpu, oracle, (1 << 20) + 13, "long", seed=9)
