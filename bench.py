@@ -1,0 +1,476 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 CVL library on the segmented float64 workload.
+
+Workload (one step): the segmented exclusive +-scan (add_sed) and the
+segmented +-reduce (add_red) of 2^28 float64 N(0,1) values whose segment
+lengths are round(LogNormal(mu=5, sigma=2)) clipped to [1, 2^24] -- the
+primitive part of the "plain GPU drop-in at scale" configuration.  Each step
+processes 2 x 2^28 elements; value = elements / second (Gelem/s).
+
+Printed as one JSON line (rank 0).  Besides the headline it carries:
+  roofline     -- the add_sed scan kernel: algorithmic bytes per launch
+                  (16 B/element + 4 B/segment) / its CUDA-event time, against
+                  the measured HBM copy bandwidth of MEASURED_PEAKS.json
+  e2e          -- the same step through the C ABI with pinned host buffers:
+                  c2v_fud upload of the values, both primitives, v2c_fud of
+                  both results, per step
+  cpu_baseline -- the CPU oracle (plain-C restatement of the serial CVL)
+                  on one host core over the same workload
+  primitives   -- Gelem/s and roofline fraction of the other CVL primitives
+                  at 2^28 elements (int32 unless named)
+  clocks       -- nvidia-smi samples taken during the timed region
+
+``--impl reference`` times the CPU implementation of the same step (the
+oracle restatement of the serial CVL; the reference sources are not on this
+machine) on all host cores, splitting the segments across threads.
+
+Multi-GPU: the workload does not exchange data between GPUs, so N GPUs run
+N independent replicas (one process per GPU under torchrun); value is the
+total over replicas divided by the slowest replica's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+LOG2N = 28
+SEED = 0x5EED + 1
+METRIC = "CVL primitive Gelem/s (segmented +_scan and +_reduce, float64)"
+UNIT = "Gelem/s"
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def segment_lengths(n):
+    from neslgpu_gb300 import workloads as W
+    return W.lognormal_lengths(W.rng(SEED), n, 5.0, 2.0, 1 << 24)
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("timestamp,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.out = ""
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                self.out, _ = self.proc.communicate()
+
+    def summary(self, t0=None, t1=None):
+        """Median SM clock and active throttle reasons over the samples whose
+        timestamps fall inside [t0, t1] (host wall-clock seconds)."""
+        import datetime as dt
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        total = 0
+        for line in (getattr(self, "out", "") or "").splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                ts = dt.datetime.strptime(f[0], "%Y/%m/%d %H:%M:%S.%f").timestamp()
+                clk, cmax = float(f[1]), float(f[2])
+            except ValueError:
+                continue
+            total += 1
+            if t0 is not None and not (t0 - 0.05 <= ts <= t1 + 0.05):
+                continue
+            sm.append(clk)
+            mx = max(mx, cmax)
+            for nm, v in zip(names, f[4:8]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples_in_window": len(sm), "samples": total}
+
+
+def dist():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as td
+        td.init_process_group("gloo")
+        pg = td
+    return world, rank, local, pg
+
+
+def allmax(pg, v):
+    if pg is None:
+        return v
+    import torch
+    t = torch.tensor([float(v)], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+# ------------------------------------------------------------ GPU arm ---
+class Gpu:
+    def __init__(self):
+        from neslgpu_gb300.cvl import load, check
+        self.c = load()
+        self.check = check
+
+    def alloc(self, units):
+        p = self.c.alo_foz(int(units))
+        if not p:
+            raise RuntimeError(self.c.gcvl_error_string().decode())
+        return p
+
+    def events(self, k):
+        return [self.c.gcvl_event_create() for _ in range(k)]
+
+    def ms(self, a, b):
+        return self.c.gcvl_event_elapsed_ms(a, b)
+
+
+def timed(g, fn, reps=5):
+    """Median CUDA-event time (ms) of fn() after one warm-up call."""
+    fn()
+    e = g.events(2)
+    ts = []
+    for _ in range(reps):
+        g.c.gcvl_event_record(e[0])
+        fn()
+        g.c.gcvl_event_record(e[1])
+        ts.append(g.ms(e[0], e[1]))
+    return statistics.median(ts)
+
+
+def primitive_suite(g, n, hbm):
+    """Gelem/s and roofline fraction of the other CVL primitives at n."""
+    from neslgpu_gb300 import workloads as W
+    c = g.c
+    out = {}
+    xi, yi, dz = g.alloc(c.siz_foz(n)), g.alloc(c.siz_foz(n)), g.alloc(c.siz_foz(n))
+    fl, ix = g.alloc(c.siz_foz(n)), g.alloc(c.siz_foz(n))
+    c.gcvl_fill_random(xi, n, 0, 11, 0.0, 0)
+    c.gcvl_fill_random(yi, n, 0, 12, 0.0, 0)
+    c.gcvl_fill_random(fl, n, 2, 13, 0.5, 0)
+    lens = W.geometric_lengths(W.rng(SEED), n, 64).astype(np.int32)
+    m = len(lens)
+    lv = g.alloc(c.siz_foz(m))
+    c.c2v_fuz(lv, lens.ctypes.data, m, None)
+    sd = g.alloc(c.siz_fos(n, m))
+    scr = g.alloc(max(c.mke_fov_scratch(n, m), c.add_sez_scratch(n, m), c.max_rez_scratch(n, m),
+                      c.pk2_luz_scratch(n), c.rku_luz_scratch(n), c.pk1_lev_scratch(n, m)))
+    c.mke_fov(sd, lv, n, m, scr)
+    # a uniform random permutation: the rank of uniform random keys
+    c.rku_luz(ix, yi, n, scr)
+    red = g.alloc(c.siz_foz(m))
+    cnt = c.pk1_luv(fl, n, scr)
+
+    def rec(name, fn, bytes_per_elem, extra=0.0):
+        t = timed(g, fn)
+        gb = (bytes_per_elem * n + extra) / (t * 1e-3) / 1e9
+        out[name] = {"gelem_s": round(n / (t * 1e-3) / 1e9, 2), "ms": round(t, 4),
+                     "achieved_gbs": round(gb, 1), "frac": round(gb / hbm, 3)}
+
+    rec("add_sez", lambda: c.add_sez(dz, xi, sd, n, m, scr), 8, 4.0 * m)
+    rec("add_sez+add_wuz (inclusive)", lambda: (c.add_sez(dz, xi, sd, n, m, scr),
+                                                c.add_wuz(dz, dz, xi, n, None)), 20, 4.0 * m)
+    rec("max_rez", lambda: c.max_rez(red, xi, sd, n, m, scr), 4, 8.0 * m)
+    rec("pk1_lev+pk2_lez (pack)", lambda: (c.pk1_lev(red, fl, sd, n, m, scr),
+                                           c.pk2_lez(dz, xi, fl, sd, n, m, sd, cnt, m, scr)), 8, 4.0 * cnt + 8.0 * m)
+    rec("smp_puz (permute)", lambda: c.smp_puz(dz, xi, ix, n, None), 12)
+    rec("bck_puz (back-permute)", lambda: c.bck_puz(dz, xi, ix, n, n, None), 12)
+    rec("add_wuz", lambda: c.add_wuz(dz, xi, yi, n, None), 12)
+    t = timed(g, lambda: c.rku_luz(dz, xi, n, scr), reps=3)
+    io, passes = 8.0, 76.0
+    out["rku_luz (rank)"] = {"gelem_s": round(n / (t * 1e-3) / 1e9, 2), "ms": round(t, 4),
+                             "achieved_gbs_io_floor": round(io * n / (t * 1e-3) / 1e9, 1),
+                             "frac_io_floor": round(io * n / (t * 1e-3) / 1e9 / hbm, 3),
+                             "frac_pass_traffic_76B": round(passes * n / (t * 1e-3) / 1e9 / hbm, 3)}
+    g.check(c)
+    for p in (xi, yi, dz, fl, ix, lv, sd, scr, red):
+        c.fre_fov(p)
+    return out
+
+
+def cpu_baseline_port(x, lens, threads=1):
+    """The oracle restatement of the serial CVL on this host: add_sed and
+    add_red over the same values and segments.  With threads > 1 the
+    segments are split into contiguous groups, one per thread (ctypes
+    releases the GIL, so the C loops run in parallel)."""
+    from oracle.oracle import load_oracle
+    o = load_oracle()
+    n, m = len(x), len(lens)
+    scan = np.empty(n)
+    red = np.empty(m)
+    cuts = [0]
+    if threads > 1:
+        c = np.cumsum(lens, dtype=np.int64)
+        for t in range(1, threads):
+            cuts.append(int(np.searchsorted(c, n * t // threads)))
+    cuts.append(m)
+    starts = np.concatenate([[0], np.cumsum(lens, dtype=np.int64)])
+
+    def work(a, b):
+        if b <= a:
+            return
+        e0, e1 = int(starts[a]), int(starts[b])
+        sd = np.ascontiguousarray(lens[a:b])
+        xs = x[e0:e1]
+        o.add_sed(scan[e0:].ctypes.data, xs.ctypes.data, sd.ctypes.data, e1 - e0, b - a, None)
+        o.add_red(red[a:].ctypes.data, xs.ctypes.data, sd.ctypes.data, e1 - e0, b - a, None)
+
+    t0 = time.perf_counter()
+    ths = [threading.Thread(target=work, args=(cuts[i], cuts[i + 1])) for i in range(len(cuts) - 1)]
+    for th in ths:
+        th.start()
+    for th in ths:
+        th.join()
+    return time.perf_counter() - t0, scan, red
+
+
+def gpu_arm(a):
+    world, rank, local, pg = dist()
+    os.environ.setdefault("GCVL_DEVICE", str(local))
+    g = Gpu()
+    c = g.c
+    hbm, peak_kind = peaks()
+    n = 1 << a.log2n
+    lens = segment_lengths(n)
+    m = len(lens)
+
+    # device-resident inputs
+    x = g.alloc(c.siz_fod(n))
+    c.gcvl_fill_random(x, n, 1, SEED, 0.0, 0)
+    lv = g.alloc(c.siz_foz(m))
+    c.c2v_fuz(lv, lens.ctypes.data, m, None)
+    sd = g.alloc(c.siz_fos(n, m))
+    scr = g.alloc(max(c.mke_fov_scratch(n, m), c.add_sed_scratch(n, m), c.add_red_scratch(n, m)))
+    c.mke_fov(sd, lv, n, m, scr)
+    ys = g.alloc(c.siz_fod(n))
+    yr = g.alloc(c.siz_fod(m))
+    g.check(c)
+
+    e_sed = [g.events(2) for _ in range(a.steps)]
+    e_red = [g.events(2) for _ in range(a.steps)]
+    e_all = g.events(2)
+
+    def step(i=None):
+        if i is not None:
+            c.gcvl_event_record(e_sed[i][0])
+        c.add_sed(ys, x, sd, n, m, scr)
+        if i is not None:
+            c.gcvl_event_record(e_sed[i][1])
+            c.gcvl_event_record(e_red[i][0])
+        c.add_red(yr, x, sd, n, m, scr)
+        if i is not None:
+            c.gcvl_event_record(e_red[i][1])
+
+    for _ in range(a.warmup):
+        step()
+    g.check(c)
+    barrier(pg)
+    clk = Clocks(local)
+    with clk:
+        time.sleep(1.0)  # let the sampler start
+        c.gcvl_sync()
+        barrier(pg)
+        l0 = c.gcvl_launch_count()
+        w0 = time.time()
+        c.gcvl_event_record(e_all[0])
+        for i in range(a.steps):
+            step(i)
+        c.gcvl_event_record(e_all[1])
+        c.gcvl_sync()
+        w1 = time.time()
+        launches = c.gcvl_launch_count() - l0
+        barrier(pg)
+        time.sleep(0.2)
+    g.check(c)
+    ms_total = allmax(pg, g.ms(e_all[0], e_all[1]))
+    ms_step = ms_total / a.steps
+    t_sed = statistics.mean(g.ms(*e) for e in e_sed)
+    t_red = statistics.mean(g.ms(*e) for e in e_red)
+    value = world * 2 * n / (ms_step * 1e-3) / 1e9
+
+    # roofline of the dominant kernel (the add_sed scan)
+    alg_bytes = 16.0 * n + 4.0 * m
+    achieved = alg_bytes / (t_sed * 1e-3) / 1e9
+    traffic = None
+    tf = ROOT / "profiles" / "ncu_traffic.json"
+    if tf.exists():
+        try:
+            traffic = json.loads(tf.read_text()).get("add_sed_bytes_per_launch")
+        except (ValueError, OSError):
+            traffic = None
+    roofline = {"bound": "hbm", "kernel": "k_scan<AddD,scan,segmented> (add_sed)",
+                "achieved": round(achieved, 1), "peak": hbm, "peak_kind": peak_kind, "unit": "GB/s",
+                "frac": round(achieved / hbm, 4), "traffic": traffic,
+                "alg_bytes_per_launch": alg_bytes,
+                "add_red": {"ms": round(t_red, 4),
+                            "achieved": round((8.0 * n + 12.0 * m) / (t_red * 1e-3) / 1e9, 1)}}
+
+    # end to end through the C ABI with pinned host buffers
+    e2e = None
+    if a.e2e_steps > 0:
+        hx = c.gcvl_host_alloc(8 * n)
+        hs = c.gcvl_host_alloc(8 * n)
+        hr = c.gcvl_host_alloc(8 * m)
+        c.v2c_fud(hx, x, n, None)  # the same values, now on the host
+        for _ in range(2):
+            c.c2v_fud(x, hx, n, None)
+            step()
+            c.v2c_fud(hs, ys, n, None)
+            c.v2c_fud(hr, yr, m, None)
+        barrier(pg)
+        c.gcvl_sync()
+        t0 = time.perf_counter()
+        for _ in range(a.e2e_steps):
+            c.c2v_fud(x, hx, n, None)
+            step()
+            c.v2c_fud(hs, ys, n, None)
+            c.v2c_fud(hr, yr, m, None)
+        c.gcvl_sync()
+        dt = allmax(pg, (time.perf_counter() - t0) / a.e2e_steps)
+        e2e = {"value": round(world * 2 * n / dt / 1e9, 3), "unit": UNIT, "ms_per_step": round(dt * 1e3, 3),
+               "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n + 8 * m,
+               "api": "c2v_fud, add_sed, add_red, v2c_fud x2 (pinned host buffers)"}
+        g.check(c)
+
+    cpu = None
+    if rank == 0 and world == 1 and not a.no_cpu:
+        xh = np.empty(n)
+        c.v2c_fud(xh.ctypes.data, x, n, None)
+        t, scan, red = cpu_baseline_port(xh, lens, threads=1)
+        cpu = {"value": round(2 * n / t / 1e9, 4), "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": f"the full workload once (add_sed + add_red over 2^{a.log2n} float64, {m} segments), "
+                         "oracle restatement of the serial CVL, 1 thread"}
+        # the GPU results of the timed steps against the CPU ones
+        gs = np.empty(n)
+        c.v2c_fud(gs.ctypes.data, ys, n, None)
+        gr = np.empty(m)
+        c.v2c_fud(gr.ctypes.data, yr, m, None)
+        cpu["max_rel_diff_scan"] = float(np.max(np.abs(gs - scan) / np.maximum(np.abs(scan), 1.0)))
+        cpu["max_rel_diff_reduce"] = float(np.max(np.abs(gr - red) / np.maximum(np.abs(red), 1.0)))
+
+    prims = None
+    if not a.no_suite and rank == 0:
+        prims = primitive_suite(g, n, hbm)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world,
+            "steps": a.steps, "warmup": a.warmup, "ms_per_step": round(ms_step, 4),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (device-generated N(0,1) values, seeded; host-generated segment lengths)",
+            "config": {"workload": f"add_sed + add_red, 2^{a.log2n} float64 N(0,1), segment lengths "
+                                   "round(LogNormal(5,2)) clipped to [1, 2^24]",
+                       "n": n, "m": m, "elements_per_step": 2 * n,
+                       "l2": "inputs larger than L2 (2 GiB per vector), no flush",
+                       "parallelism": f"{world} independent replicas"},
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
+            "clocks": clk.summary(w0, w1), "primitives": prims,
+        }
+        print(json.dumps(line))
+
+
+# ------------------------------------------------------ reference arm ---
+def reference_arm(a):
+    world, rank, local, pg = dist()
+    if rank != 0:
+        return
+    from neslgpu_gb300 import workloads as W
+    n = 1 << a.log2n
+    lens = segment_lengths(n)
+    m = len(lens)
+    cores = os.cpu_count() or 1
+    x = W.float64_normal(W.rng(SEED), n)
+    times = []
+    for _ in range(a.warmup if a.warmup < 2 else 1):
+        cpu_baseline_port(x, lens, threads=cores)
+    for _ in range(a.steps):
+        t, _, _ = cpu_baseline_port(x, lens, threads=cores)
+        times.append(t)
+    t = statistics.median(times)
+    v = round(2 * n / t / 1e9, 4)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world,
+        "steps": a.steps, "warmup": a.warmup, "ms_per_step": round(t * 1e3, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (host-generated, seeded)",
+        "config": {"workload": f"add_sed + add_red, 2^{a.log2n} float64 N(0,1), segment lengths "
+                               "round(LogNormal(5,2)) clipped to [1, 2^24]", "n": n, "m": m,
+                   "elements_per_step": 2 * n},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": "the full workload per step; segments split across all host threads; "
+                                   "the serial CVL's algorithm as restated by the oracle (the reference "
+                                   "sources are not present on this machine)"},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=500)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--log2n", type=int, default=LOG2N)
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-suite", action="store_true")
+    ap.add_argument("--suite-only", action="store_true",
+                    help="only the per-primitive table at 2^log2n (for profiling)")
+    a = ap.parse_args()
+    a.warmup = max(a.warmup, 3) if a.impl == "gb300" else a.warmup
+    if a.impl == "reference":
+        a.steps = min(a.steps, 5)
+        reference_arm(a)
+    elif a.suite_only:
+        g = Gpu()
+        print(json.dumps({"primitives": primitive_suite(g, 1 << a.log2n, peaks()[0])}))
+    else:
+        gpu_arm(a)
+
+
+if __name__ == "__main__":
+    main()

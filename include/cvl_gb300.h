@@ -738,6 +738,12 @@ void *gcvl_host_alloc(size_t bytes);
 void gcvl_host_free(void *p);
 void gcvl_h2d_async(vec_p d, const void *s, size_t bytes);
 void gcvl_d2h_async(void *d, vec_p s, size_t bytes);
+/* Kernels launched by this library so far (all entry points). */
+unsigned long long gcvl_launch_count(void);
+/* Seeded synthetic vector on the device (benchmark inputs); element i
+ * depends only on (seed, i).  kind 0: int32 uniform over all values,
+ * 1: float64 N(0,1), 2: cvl_bool Bernoulli(a), 3: int32 uniform in [0, b). */
+void gcvl_fill_random(vec_p d, long n, int kind, unsigned long long seed, double a, int b);
 /* The 48-bit lrand48 state behind rnd_wuz. */
 unsigned long long gcvl_rand_state(void);
 void gcvl_set_rand_state(unsigned long long state);

@@ -126,14 +126,22 @@ struct MulD { typedef double T;
 __host__ __device__ inline double bits_to_double(unsigned long long v) {
   union { unsigned long long l; double d; } u; u.l = v; return u.d;
 }
+// Order key of a double: signed-integer order equals the double order for
+// non-NaN values, with -0.0 and +0.0 equal (as == has them).  Min and max
+// compare keys so that they run on the integer pipes, not the FP64 pipe.
+__device__ __forceinline__ long long dkey(double x) {
+  long long b = __double_as_longlong(x);
+  if ((b << 1) == 0) return 0;
+  return b ^ ((b >> 63) & 0x7FFFFFFFFFFFFFFFLL);
+}
 struct MinD { typedef double T;
   __host__ __device__ static T init() { return (double)(float)1.0e36; }
   __host__ __device__ static T ident() { return bits_to_double(0x7FF0000000000000ULL); }
-  __device__ static T apply(T a, T b) { return a < b ? a : b; } };
+  __device__ static T apply(T a, T b) { return dkey(a) < dkey(b) ? a : b; } };
 struct MaxD { typedef double T;
   __host__ __device__ static T init() { return (double)(float)-1.0e36; }
   __host__ __device__ static T ident() { return bits_to_double(0xFFF0000000000000ULL); }
-  __device__ static T apply(T a, T b) { return a > b ? a : b; } };
+  __device__ static T apply(T a, T b) { return dkey(a) > dkey(b) ? a : b; } };
 // pk1_lev counts true flags per segment: an add over (x != 0).
 struct CountB { typedef int T;
   __host__ __device__ static T init() { return 0; }

@@ -34,7 +34,9 @@ bool check_cuda(cudaError_t e, const char *what) {
   return false;
 }
 
+static unsigned long long g_launches = 0;
 void launch_check(const char *what) {
+  ++g_launches;
   cudaError_t e = cudaPeekAtLastError();
   if (e != cudaSuccess) {
     cudaGetLastError();
@@ -121,6 +123,45 @@ GCVL_EXPORT void gcvl_set_stream(void *stream) {
   if (stream) { s.stream = (cudaStream_t)stream; s.own_stream = false; }
   else if (own) { s.stream = own; s.own_stream = true; }
 }
+// Number of kernels this library has launched (all entry points).
+GCVL_EXPORT unsigned long long gcvl_launch_count(void) { return gcvl::g_launches; }
+
+// Seeded synthetic vectors generated on the device (benchmark inputs):
+// element i depends only on (seed, i) through splitmix64.
+//   kind 0: int32 uniform over all values      kind 1: float64 N(0,1)
+//   kind 2: cvl_bool Bernoulli(p = a)           kind 3: int32 uniform [0, b)
+__device__ __forceinline__ unsigned long long splitmix64(unsigned long long x) {
+  x += 0x9E3779B97F4A7C15ULL;
+  x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  x = (x ^ (x >> 27)) * 0x94D049BB133111EBULL;
+  return x ^ (x >> 31);
+}
+__global__ void k_fill_random(void *d, long n, int kind, unsigned long long seed, double a, int b) {
+  const long stride = (long)gridDim.x * blockDim.x;
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    unsigned long long h = splitmix64(seed * 0x632BE59BD9B4E019ULL + (unsigned long long)i);
+    if (kind == 0) {
+      ((int *)d)[i] = (int)(unsigned)(h >> 32);
+    } else if (kind == 1) {
+      // Box-Muller on two 53-bit uniforms
+      unsigned long long h2 = splitmix64(h);
+      double u1 = ((h >> 11) + 1) * 0x1.0p-53, u2 = (h2 >> 11) * 0x1.0p-53;
+      ((double *)d)[i] = sqrt(-2.0 * log(u1)) * cospi(2.0 * u2);
+    } else if (kind == 2) {
+      ((int *)d)[i] = ((h >> 11) * 0x1.0p-53) < a ? 1 : 0;
+    } else {
+      ((int *)d)[i] = (int)((h >> 32) % (unsigned long long)(b > 0 ? b : 1));
+    }
+  }
+}
+GCVL_EXPORT void gcvl_fill_random(vec_p d, long n, int kind, unsigned long long seed, double a, int b) {
+  ensure_init();
+  if (n <= 0) return;
+  long g = (n + 255) / 256, cap = (long)st().sm_count * 32;
+  k_fill_random<<<(int)(g < cap ? g : cap), 256, 0, st().stream>>>(d, n, kind, seed, a, b);
+  launch_check("k_fill_random");
+}
+
 GCVL_EXPORT int gcvl_sm_count(void) { ensure_init(); return st().sm_count; }
 GCVL_EXPORT int gcvl_device(void) { ensure_init(); return st().device; }
 // Iteration limit of every bounded device wait; a small value makes waits

@@ -12,6 +12,10 @@
 // with short segments no CTA ever waits; long segments wait on a chain that
 // the warp-wide look-back walks 32 tiles at a time.  Every wait is bounded.
 #include "gcvl.cuh"
+#include "tma.cuh"
+
+#include <stdlib.h>
+#include <type_traits>
 
 namespace gcvl {
 
@@ -262,6 +266,423 @@ k_scan(ScanArgs<typename Op::T> a) {
   }
 }
 
+// ============================================================================
+// TMA-staged single-pass kernel (the fast path for 16-byte aligned vectors).
+//
+// A tile is 256 rows of 128 bytes (32 ints or 16 doubles per row), one row
+// per thread.  One elected thread moves the whole tile with a 2-D TMA tensor
+// copy (128-byte swizzle, so each thread reads its row from shared memory
+// without bank conflicts) and writes scan results back the same way.
+// Segment heads come from a window of the segment offsets that the CTA
+// loads once into shared memory.  Float64 + folds run in 128-bit integer
+// fixed point and float64 min/max compare integer keys, which keeps the
+// GB300's narrow FP64 pipe free for the one add per element that an
+// exclusive scan output needs.
+// ============================================================================
+constexpr int TT = 256;    // threads per CTA = rows per tile
+constexpr int WMAX = 2048; // offsets window held in shared memory
+template <class T> constexpr int row_items() { return 128 / (int)sizeof(T); }
+
+template <class T> struct TArgs {
+  T *out;
+  const T *in;
+  SegView sv;
+  int n;
+  long rows;  // complete 128-byte rows of the input (the TMA tensor height)
+  LookbackMem lb;
+  unsigned *status;
+  int spin_limit;
+};
+
+// Segment offsets seen through the shared-memory window when possible.
+struct OffWin {
+  const int *win; const int *glob; int s0, w;
+  __device__ __forceinline__ int operator()(int s) const {
+    int j = s - s0;
+    return (j >= 0 && j < w) ? win[j] : __ldg(glob + s);
+  }
+};
+
+// ---- per-thread fold engines ---------------------------------------------
+// agg(): (has head, fold of the items from the last head -- starting from
+// init -- or of all items when there is none).
+template <class Op, int ITEMS> struct Engine {
+  typedef typename Op::T T;
+  static __device__ __forceinline__ void agg(const T (&x)[ITEMS], unsigned heads, int cnt, int &tf, T &tv) {
+    tf = heads != 0;
+    tv = Op::ident();
+#pragma unroll
+    for (int i = 0; i < ITEMS; i++)
+      if (i < cnt) tv = ((heads >> i) & 1u) ? Op::apply(Op::init(), x[i]) : Op::apply(tv, x[i]);
+  }
+};
+
+template <int ITEMS> struct Engine<AddD, ITEMS> {
+  static __device__ __forceinline__ void agg(const double (&x)[ITEMS], unsigned heads, int cnt, int &tf,
+                                             double &tv) {
+    tf = heads != 0;
+    tv = AddD::ident();
+    if (cnt <= 0) return;
+    const int from = heads ? 31 - __clz((int)heads) : 0;
+    int emax = 1;
+#pragma unroll
+    for (int i = 0; i < ITEMS; i++)
+      if (i >= from && i < cnt) emax = max(emax, fx_exp((unsigned long long)__double_as_longlong(x[i])));
+    if (emax == 2047) {  // an infinity or NaN: fold in FP64
+#pragma unroll
+      for (int i = 0; i < ITEMS; i++)
+        if (i >= from && i < cnt) tv = (i == from && tf) ? AddD::apply(0.0, x[i]) : AddD::apply(tv, x[i]);
+      return;
+    }
+    Fx128 acc{0ULL, 0ULL};
+#pragma unroll
+    for (int i = 0; i < ITEMS; i++)
+      if (i >= from && i < cnt) fx_add(acc, (unsigned long long)__double_as_longlong(x[i]), emax);
+    tv = fx_to_double(acc, emax);  // never -0.0, so starting from init 0.0 changes nothing
+  }
+};
+
+// Sum of x[from..to) by the fixed-point path (FP64 when inf/NaN present).
+template <int ITEMS>
+__device__ __forceinline__ double fx_range(const double (&x)[ITEMS], int from, int to) {
+  int emax = 1;
+#pragma unroll
+  for (int i = 0; i < ITEMS; i++)
+    if (i >= from && i < to) emax = max(emax, fx_exp((unsigned long long)__double_as_longlong(x[i])));
+  if (emax == 2047) {
+    double v = -0.0;
+#pragma unroll
+    for (int i = 0; i < ITEMS; i++)
+      if (i >= from && i < to) v = __dadd_rn(v, x[i]);
+    return v;
+  }
+  Fx128 acc{0ULL, 0ULL};
+#pragma unroll
+  for (int i = 0; i < ITEMS; i++)
+    if (i >= from && i < to) fx_add(acc, (unsigned long long)__double_as_longlong(x[i]), emax);
+  return fx_to_double(acc, emax);
+}
+
+template <class Op, int MODE, bool SEG>
+__global__ void __launch_bounds__(TT) k_scan_tma(const __grid_constant__ CUtensorMap tin,
+                                                 const __grid_constant__ CUtensorMap tout,
+                                                 TArgs<typename Op::T> a) {
+  typedef typename Op::T T;
+  constexpr int ITEMS = row_items<T>(), TILE = TT * ITEMS, NW = TT / 32;
+  extern __shared__ unsigned char dyn_smem[];
+  unsigned char *tile_b = (unsigned char *)(((size_t)dyn_smem + 1023) & ~(size_t)1023);
+  int *win = (int *)(tile_b + TILE * sizeof(T));
+  __shared__ unsigned long long bar;
+  __shared__ int s_wf[NW], s_wpf[NW];
+  __shared__ T s_wv[NW], s_wpv[NW];
+  __shared__ T s_prefix;
+  __shared__ unsigned s_tile;
+  __shared__ int s_sfirst, s_slast;
+
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (tid == 0) {
+    s_tile = atomicAdd(a.lb.counter, 1u);
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  const int tile = (int)s_tile;
+  const long base = (long)tile * TILE;
+  const int valid = (int)min((long)TILE, (long)a.n - base);
+  if (tid == 0) {
+    mbar_arrive_expect_tx(&bar, TILE * (unsigned)sizeof(T));
+    tma_load_2d(tile_b, &tin, &bar, 0, tile * TT);
+  }
+  if (SEG) {
+    if (tid == 0) s_sfirst = seg_of(a.sv, (int)base);
+    if (tid == 32) s_slast = seg_of(a.sv, (int)base + valid - 1);
+  }
+  __syncthreads();
+  int W = 0, sf = 0;
+  if (SEG) {
+    sf = s_sfirst;
+    W = s_slast - sf + 2;
+    if (W <= WMAX)
+      for (int i = tid; i < W; i += TT) win[i] = __ldg(a.sv.off + sf + i);
+  }
+  {
+    int it = 0;
+    while (!mbar_try_wait(&bar, 0)) {
+      if (++it >= a.spin_limit) { atomicOr(a.status, DEV_TIMEOUT); break; }
+    }
+  }
+  __syncthreads();
+  const OffWin off{win, a.sv.off, sf, (SEG && W <= WMAX) ? W : 0};
+
+  // this thread's row
+  const int k0 = (int)base + tid * ITEMS;
+  const int cnt = max(0, min(ITEMS, a.n - k0));
+  const long grow = (long)tile * TT + tid;
+  T x[ITEMS];
+  if (grow < a.rows) {
+#pragma unroll
+    for (int c = 0; c < 8; c++) {
+      const uint4 u = *(const uint4 *)(tile_b + swz(tid, c));
+      memcpy(&x[c * (16 / sizeof(T))], &u, 16);
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < ITEMS; i++) x[i] = (i < cnt) ? a.in[k0 + i] : Op::ident();
+  }
+
+  // segment heads of the row
+  unsigned heads = 0;
+  int s0 = 0;
+  if (cnt > 0) {
+    if (SEG) {
+      if (W <= WMAX) {
+        int lo = 0, hi = W - 2;  // window index of the segment holding k0
+        while (lo < hi) {
+          int mid = (lo + hi + 1) >> 1;
+          if (win[mid] <= k0) lo = mid; else hi = mid - 1;
+        }
+        s0 = sf + lo;
+        if (win[lo] == k0) heads = 1u;
+        int j = lo, nxt = win[j + 1];
+        while (nxt < k0 + cnt) {
+          heads |= 1u << (nxt - k0);
+          ++j;
+          while (win[j + 1] == nxt) ++j;
+          nxt = win[j + 1];
+        }
+      } else {
+        heads = head_bits<ITEMS>(a.sv, k0, cnt, s0);
+      }
+    } else {
+      heads = (k0 == 0) ? 1u : 0u;
+    }
+  }
+
+  int tf;
+  T tv;
+  Engine<Op, ITEMS>::agg(x, heads, cnt, tf, tv);
+
+  // warp inclusive scan of (head, value)
+  int f = tf;
+  T v = tv;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    int f2 = shfl_up(f, d);
+    T v2 = shfl_up(v, d);
+    if (lane >= d) { v = f ? v : Op::apply(v2, v); f |= f2; }
+  }
+  int ef = shfl_up(f, 1);
+  T ev = shfl_up(v, 1);
+  if (lane == 0) { ef = 0; ev = Op::ident(); }
+  if (lane == 31) { s_wf[warp] = f; s_wv[warp] = v; }
+  __syncthreads();
+
+  if (warp == 0) {
+    // exclusive prefixes over the warps and the tile aggregate
+    int wf = lane < NW ? s_wf[lane] : 0;
+    T wv = lane < NW ? s_wv[lane] : Op::ident();
+#pragma unroll
+    for (int d = 1; d < NW; d <<= 1) {
+      int f2 = shfl_up(wf, d);
+      T v2 = shfl_up(wv, d);
+      if (lane >= d) { wv = wf ? wv : Op::apply(v2, wv); wf |= f2; }
+    }
+    int xf = shfl_up(wf, 1);
+    T xv = shfl_up(wv, 1);
+    if (lane == 0) { xf = 0; xv = Op::ident(); }
+    if (lane < NW) { s_wpf[lane] = xf; s_wpv[lane] = xv; }
+    const int af = shfl_idx(wf, NW - 1);
+    const T av = shfl_idx(wv, NW - 1);
+    const bool first_head = shfl_idx((int)(heads & 1u), 0) != 0;
+    if (lane == 0) {
+      if (tile == 0 || af) {
+        st_relaxed(a.lb.inc + tile, to_bits<T>(av));
+        st_release(a.lb.flags + tile, TS_INC);
+      } else {
+        st_relaxed(a.lb.agg + tile, to_bits<T>(av));
+        st_release(a.lb.flags + tile, TS_AGG);
+      }
+    }
+    T P = Op::ident();
+    if (tile > 0 && !first_head) {
+      int pred = tile - 1;
+      while (true) {
+        int t = pred - lane;
+        unsigned fl = TS_INC;
+        T val = Op::ident();
+        if (t >= 0) {
+          int it = 0;
+          fl = ld_acquire(a.lb.flags + t);
+          while (fl == TS_EMPTY) {
+            if (++it >= a.spin_limit) break;
+            __nanosleep(32);
+            fl = ld_acquire(a.lb.flags + t);
+          }
+          if (fl == TS_EMPTY) { atomicOr(a.status, DEV_TIMEOUT); fl = TS_INC; }
+          else val = from_bits<T>(ld_relaxed(fl == TS_INC ? a.lb.inc + t : a.lb.agg + t));
+        }
+        unsigned incm = __ballot_sync(0xffffffffu, fl == TS_INC);
+        int stop = incm ? __ffs(incm) - 1 : 31;
+        if (lane > stop) val = Op::ident();
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+          T o = shfl_down(val, d);
+          if (lane + d < 32) val = Op::apply(o, val);
+        }
+        val = shfl_idx(val, 0);
+        P = Op::apply(val, P);
+        if (incm) break;
+        pred -= 32;
+      }
+      if (lane == 0 && !af) {
+        st_relaxed(a.lb.inc + tile, to_bits<T>(Op::apply(P, av)));
+        st_release(a.lb.flags + tile, TS_INC);
+      }
+    }
+    if (lane == 0) s_prefix = P;
+  }
+  __syncthreads();
+  // this thread's exclusive prefix: (earlier tiles) . (earlier warps) . (earlier lanes)
+  int pf = s_wpf[warp];
+  T pv = s_wpv[warp];
+  pv = ef ? ev : Op::apply(pv, ev);
+  pf |= ef;
+  T run = pf ? pv : Op::apply(s_prefix, pv);
+
+  if (MODE == M_SCAN) {
+#pragma unroll
+    for (int i = 0; i < ITEMS; i++) {
+      if ((heads >> i) & 1u) run = Op::init();
+      const T y = run;
+      run = Op::apply(run, x[i]);
+      x[i] = y;
+    }
+    if (grow < a.rows) {
+#pragma unroll
+      for (int c = 0; c < 8; c++) {
+        uint4 u;
+        memcpy(&u, &x[c * (16 / sizeof(T))], 16);
+        *(uint4 *)(tile_b + swz(tid, c)) = u;
+      }
+    } else {
+#pragma unroll
+      for (int i = 0; i < ITEMS; i++)
+        if (i < cnt) a.out[k0 + i] = x[i];
+    }
+    fence_proxy_async_smem();
+    __syncthreads();
+    if (tid == 0) {
+      tma_store_2d(&tout, tile_b, 0, tile * TT);
+      bulk_commit();
+      bulk_wait_read_all();
+    }
+  } else {  // M_REDUCE: results at segment ends
+    if (cnt > 0) {
+      const int m = a.sv.m;
+      if (k0 == 0)
+        for (int s = 0; s < s0; s++) a.out[s] = Op::init();
+      int s = s0;
+      int end = off(s + 1);
+      if constexpr (std::is_same<Op, AddD>::value) {
+        // pieces between heads, each summed in fixed point
+        int ps = 0;
+        for (int i = 0; i < cnt; i++) {
+          if (k0 + i + 1 == end) {
+            double pv2 = fx_range<ITEMS>(x, ps, i + 1);
+            a.out[s] = ((heads >> ps) & 1u) ? pv2 : AddD::apply(run, pv2);
+            int s2 = s + 1;
+            while (s2 < m && off(s2 + 1) == end) { a.out[s2] = 0.0; ++s2; }
+            s = s2;
+            if (s < m) end = off(s + 1);
+            ps = i + 1;
+          }
+        }
+      } else {
+#pragma unroll
+        for (int i = 0; i < ITEMS; i++) {
+          if (i < cnt) {
+            if ((heads >> i) & 1u) run = Op::init();
+            run = Op::apply(run, x[i]);
+            if (k0 + i + 1 == end) {
+              a.out[s] = run;
+              int s2 = s + 1;
+              while (s2 < m && off(s2 + 1) == end) { a.out[s2] = Op::init(); ++s2; }
+              s = s2;
+              if (s < m) end = off(s + 1);
+            }
+          }
+        }
+      }
+    }
+  }
+}
+
+// Host side: tensor maps and launch.  The driver's tensor-map encoder is
+// looked up through the runtime, so the library itself does not link
+// libcuda and loads on machines without a GPU driver.
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *,
+                                  CUtensorMapInterleave, CUtensorMapSwizzle, CUtensorMapL2promotion,
+                                  CUtensorMapFloatOOBfill);
+static EncodeTiledFn encode_tiled() {
+  static EncodeTiledFn fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+      fn = (EncodeTiledFn)p;
+    else
+      cudaGetLastError();
+  }
+  return fn;
+}
+
+template <class T> bool tma_map(CUtensorMap *map, const void *ptr, long rows) {
+  EncodeTiledFn enc = encode_tiled();
+  if (!enc) return false;
+  cuuint64_t dims[2] = {(cuuint64_t)row_items<T>(), (cuuint64_t)rows};
+  cuuint64_t strides[1] = {128};
+  cuuint32_t box[2] = {(cuuint32_t)row_items<T>(), (cuuint32_t)TT};
+  cuuint32_t es[2] = {1, 1};
+  CUresult r = enc(
+      map, sizeof(T) == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_INT32, 2, (void *)ptr,
+      dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+      CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+template <class T> constexpr size_t tma_smem() { return 1024 + (size_t)TT * row_items<T>() * sizeof(T) + WMAX * 4; }
+
+// Returns false (nothing launched) when the vectors do not suit TMA.
+template <class Op, int MODE, bool SEG>
+bool run_scan_tma(typename Op::T *out, const typename Op::T *in, vec_p sd, int n, int m, vec_p scratch,
+                  const char *name) {
+  typedef typename Op::T T;
+  if (getenv("GCVL_NO_TMA")) return false;
+  const long rows = (long)n / row_items<T>();
+  if (rows < 1 || ((size_t)in & 15) || (MODE == M_SCAN && ((size_t)out & 15))) return false;
+  CUtensorMap tin, tout;
+  if (!tma_map<T>(&tin, in, rows)) return false;
+  if (MODE == M_SCAN) { if (!tma_map<T>(&tout, out, rows)) return false; }
+  else tout = tin;
+  State &S = st();
+  const int tiles = ceil_div(n, (long)TT * row_items<T>());
+  void *mem = scratch_or_work(scratch, lookback_bytes(tiles));
+  if (!mem) return true;
+  TArgs<T> a;
+  a.out = out; a.in = in; a.n = n; a.rows = rows;
+  a.sv = SEG ? seg_view(sd, n, m) : SegView{nullptr, nullptr, nullptr, n, 1};
+  a.lb = lookback_carve(mem, tiles);
+  a.status = S.d_status;
+  a.spin_limit = S.spin_limit;
+  GCVL_CK(cudaMemsetAsync(mem, 0, lookback_clear_bytes(tiles), S.stream));
+  k_scan_tma<Op, MODE, SEG><<<tiles, TT, tma_smem<T>(), S.stream>>>(tin, tout, a);
+  launch_check(name);
+  return true;
+}
+
 template <class Op>
 __global__ void k_fill(typename Op::T *out, int m) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -283,6 +704,9 @@ void run_scan(typename Op::T *out, const typename Op::T *in, typename Op::T *out
   ensure_init();
   State &S = st();
   if (n <= 0) return;
+  if constexpr (MODE == M_SCAN || MODE == M_REDUCE) {
+    if (!count_flags && run_scan_tma<Op, MODE, SEG>(out, in, sd, n, m, scratch, name)) return;
+  }
   const int tiles = ceil_div(n, tile_elems<T>());
   void *mem = scratch_or_work(scratch, lookback_bytes(tiles));
   if (!mem) return;

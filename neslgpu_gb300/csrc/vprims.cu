@@ -85,9 +85,9 @@ template <class T> struct BPerm {  // d[k] = s[i[k]]
   __device__ void operator()(long k) const { d[k] = __ldg(s + __ldg(i + k)); }
 };
 template <class T> struct BPermSeg {  // d[k] = s[off_s[seg_d(k)] + i[k]]
-  T *d; const T *s; const int *i; const int *off_s;
+  T *d; const T *s; const int *i; const int *off_s; int m_s;
   __device__ void operator()(int k, int sg, int) const {
-    d[k] = __ldg(s + (long)__ldg(off_s + sg) + __ldg(i + k));
+    if (sg < m_s) d[k] = __ldg(s + (long)__ldg(off_s + sg) + __ldg(i + k));
   }
 };
 template <class T> struct FPerm {  // if f[k]: d[i[k]] = s[k]
@@ -95,9 +95,10 @@ template <class T> struct FPerm {  // if f[k]: d[i[k]] = s[k]
   __device__ void operator()(long k) const { if (__ldg(f + k)) d[__ldg(i + k)] = __ldcs(s + k); }
 };
 template <class T> struct FPermSeg {  // if f[k]: d[off_d[seg_s(k)] + i[k]] = s[k]
-  T *d; const T *s; const int *i; const int *f; const int *off_d;
+  T *d; const T *s; const int *i; const int *f; const int *off_d; int m_d;
   __device__ void operator()(int k, int sg, int) const {
-    if (f == nullptr || __ldg(f + k)) d[(long)__ldg(off_d + sg) + __ldg(i + k)] = __ldcs(s + k);
+    if (sg < m_d && (f == nullptr || __ldg(f + k)))
+      d[(long)__ldg(off_d + sg) + __ldg(i + k)] = __ldcs(s + k);
   }
 };
 template <class T> struct BFPerm {  // d[k] = f[k] ? s[i[k]] : 0
@@ -357,7 +358,7 @@ META_SEG(ind_lez, INPLACE_NONE)
     (void)scratch; ensure_init();                                                       \
     if (m_s == 1) { each(BPerm<T>{(T *)d, (const T *)s, (const int *)i}, n_d, "bck_pe" #L); return; } \
     SegView ss = seg_view(sd_s, n_s, m_s);                                              \
-    segwalk(BPermSeg<T>{(T *)d, (const T *)s, (const int *)i, ss.off},                 \
+    segwalk(BPermSeg<T>{(T *)d, (const T *)s, (const int *)i, ss.off, m_s},                 \
             seg_view(sd_d, n_d, m_d), "bck_pe" #L);                                     \
   }                                                                                     \
   META_SEG2(bck_pe##L, INPLACE_2)                                                       \
@@ -372,7 +373,7 @@ META_SEG(ind_lez, INPLACE_NONE)
     (void)scratch; ensure_init();                                                       \
     if (m_s == 1) { fpm_pu##L(d, s, i, f, n_s, n_d, scratch); return; }                 \
     SegView sdd = seg_view(sd_d, n_d, m_d);                                             \
-    segwalk(FPermSeg<T>{(T *)d, (const T *)s, (const int *)i, (const int *)f, sdd.off}, \
+    segwalk(FPermSeg<T>{(T *)d, (const T *)s, (const int *)i, (const int *)f, sdd.off, m_d}, \
             seg_view(sd_s, n_s, m_s), "fpm_pe" #L);                                     \
   }                                                                                     \
   META_SEG2(fpm_pe##L, INPLACE_NONE)                                                    \
@@ -404,7 +405,7 @@ META_SEG(ind_lez, INPLACE_NONE)
     if (m_s == 1) { dpe_pu##L(d, s, i, v, n_s, n_d, scratch); return; }                 \
     copy_dev<T>(d, v, n_d);                                                             \
     SegView sdd = seg_view(sd_d, n_d, m_d);                                             \
-    segwalk(FPermSeg<T>{(T *)d, (const T *)s, (const int *)i, nullptr, sdd.off},        \
+    segwalk(FPermSeg<T>{(T *)d, (const T *)s, (const int *)i, nullptr, sdd.off, m_d},   \
             seg_view(sd_s, n_s, m_s), "dpe_pe" #L);                                     \
   }                                                                                     \
   META_SEG2(dpe_pe##L, INPLACE_3)                                                       \

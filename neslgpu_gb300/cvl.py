@@ -31,7 +31,7 @@ _CT = {
     "v": None, "i": C.c_int, "u": C.c_uint, "d": C.c_double, "b": C.c_int,
     "p": C.c_void_p, "I": C.c_void_p, "B": C.c_void_p, "D": C.c_void_p,
     "T": C.POINTER(Timespec), "c": C.c_char_p, "z": C.c_size_t, "P": C.c_void_p,
-    "f": C.c_float, "q": C.c_ulonglong,
+    "f": C.c_float, "q": C.c_ulonglong, "l": C.c_long,
 }
 
 
@@ -105,20 +105,25 @@ class DeviceVector:
 
     kind: 'z' int, 'b' cvl_bool, 'd' double, 'u' raw 8-byte units."""
 
-    def __init__(self, cvl: CVL, length: int, kind: str = "z", units: int | None = None):
+    def __init__(self, cvl: CVL, length: int, kind: str = "z", units: int | None = None,
+                 offset: int = 0):
+        """offset: place the vector that many 8-byte units into its
+        allocation (vinterp sub-allocates its heap in 8-byte units, so a
+        vec_p need not be 16-byte aligned)."""
         self.cvl = cvl
         self.len = int(length)
         self.kind = kind
         if units is None:
             units = {"z": cvl.siz_foz, "b": cvl.siz_fob, "d": cvl.siz_fod}[kind](self.len) if kind != "u" else self.len
         self.units = max(int(units), 1)
-        ptr = cvl.alo_foz(self.units)
-        if not ptr:
+        base = cvl.alo_foz(self.units + offset)
+        if not base:
             raise CVLError(f"alo_foz({self.units}) failed: {cvl.gcvl_error_string().decode()}")
-        self.ptr = ptr
+        self.base = base
+        self.ptr = cvl.add_fov(base, offset) if offset else base
 
     @classmethod
-    def from_numpy(cls, cvl: CVL, arr, kind: str | None = None) -> "DeviceVector":
+    def from_numpy(cls, cvl: CVL, arr, kind: str | None = None, offset: int = 0) -> "DeviceVector":
         arr = np.ascontiguousarray(arr)
         if kind is None:
             kind = _KIND.get(arr.dtype)
@@ -126,7 +131,7 @@ class DeviceVector:
                 raise TypeError(f"no CVL type for {arr.dtype}")
         dt = np.float64 if kind == "d" else np.int32
         arr = np.ascontiguousarray(arr, dtype=dt)
-        v = cls(cvl, arr.size, kind)
+        v = cls(cvl, arr.size, kind, offset=offset)
         v.upload(arr)
         return v
 
@@ -147,7 +152,7 @@ class DeviceVector:
 
     def free(self) -> None:
         if self.ptr:
-            self.cvl.fre_fov(self.ptr)
+            self.cvl.fre_fov(self.base)
             self.ptr = None
 
     def __del__(self):

@@ -23,10 +23,12 @@ def np_dtype(kind: str):
 class DeviceRunner:
     """Vectors live on the GPU heap; every call goes through the C ABI."""
 
-    def __init__(self, cvl: CVL | None = None, checked: bool = True):
+    def __init__(self, cvl: CVL | None = None, checked: bool = True, offset: int = 0):
+        """offset: allocate every vector that many 8-byte units into its
+        allocation (exercises the kernels' unaligned paths)."""
         self.cvl = cvl or load()
         self.checked = checked
-        self._keep = []
+        self.offset = offset
 
     def fn(self, name):
         return getattr(self.cvl, name)
@@ -34,14 +36,14 @@ class DeviceRunner:
     def vec(self, arr, kind):
         arr = np.ascontiguousarray(arr, dtype=np_dtype(kind))
         if arr.size == 0:
-            return DeviceVector(self.cvl, 1, kind)
-        return DeviceVector.from_numpy(self.cvl, arr, kind)
+            return DeviceVector(self.cvl, 1, kind, offset=self.offset)
+        return DeviceVector.from_numpy(self.cvl, arr, kind, offset=self.offset)
 
     def out(self, n, kind):
-        return DeviceVector(self.cvl, max(int(n), 1), kind)
+        return DeviceVector(self.cvl, max(int(n), 1), kind, offset=self.offset)
 
     def units(self, u):
-        return DeviceVector(self.cvl, 0, "u", units=max(int(u), 1))
+        return DeviceVector(self.cvl, 0, "u", units=max(int(u), 1), offset=self.offset)
 
     def p(self, h):
         return None if h is None else h.ptr

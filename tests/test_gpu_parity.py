@@ -39,3 +39,15 @@ def test_parity_segment_shapes(gpu, oracle, kind):
 def test_parity_large(gpu, oracle):
     # several tiles per segment and several segments per tile at once
     _run_all(gpu, oracle, (1 << 20) + 13, "long", seed=9)
+
+
+@pytest.mark.parametrize("kind", ["geo", "long", "empty"])
+def test_parity_unaligned_vectors(oracle, kind):
+    """Every vector 8 bytes past a 16-byte boundary, as vinterp's 8-byte
+    sub-allocation can place it: the kernels' non-TMA paths."""
+    from neslgpu_gb300.cvl import load
+    from neslgpu_gb300.ops import DeviceRunner
+    from conftest import _has_gpu
+    if not _has_gpu():
+        pytest.skip("no GPU")
+    _run_all(DeviceRunner(load(), offset=1), oracle, 70_001, kind, seed=21)
