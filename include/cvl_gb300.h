@@ -744,6 +744,22 @@ unsigned long long gcvl_launch_count(void);
  * depends only on (seed, i).  kind 0: int32 uniform over all values,
  * 1: float64 N(0,1), 2: cvl_bool Bernoulli(a), 3: int32 uniform in [0, b). */
 void gcvl_fill_random(vec_p d, long n, int kind, unsigned long long seed, double a, int b);
+/* Segmented exclusive +-scan of float64 (add_sed) that allocates nothing.
+ * No counterpart in the reference.  For callers that may not allocate device
+ * memory -- code running during CUDA graph capture, embedders whose device
+ * memory all belongs to their own pool, runtimes that forbid allocation
+ * after start-up.  Same arguments and results as add_sed minus the scratch
+ * vector: the look-back scratch is a fixed array inside the library, sized
+ * for n <= gcvl_add_sed_noalloc_max_n() (2^28 elements, about 2.6 MB, held
+ * on every GPU that loads the library until exit).  Larger n is rejected
+ * with GCVL error 5 (range) and nothing runs.  The first call on a device
+ * looks up the array's device address there, so make it before any stream
+ * capture.  The library's first-use set-up is not run; the call uses the
+ * library stream if that exists, else the legacy default stream.  Calls
+ * share the array: calls that overlap on the GPU race.  Returns 0 or a
+ * GCVL error code. */
+int gcvl_add_sed_noalloc(vec_p d, vec_p s, vec_p sd, int n, int m);
+long gcvl_add_sed_noalloc_max_n(void);
 /* The 48-bit lrand48 state behind rnd_wuz. */
 unsigned long long gcvl_rand_state(void);
 void gcvl_set_rand_state(unsigned long long state);

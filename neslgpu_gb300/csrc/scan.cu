@@ -960,3 +960,96 @@ GCVL_EXPORT int pk1_lev_scratch(int n, int m) {
   (void)m; int a = scan_units<int>(n), b = reduce_units<int>(n); return a > b ? a : b;
 }
 GCVL_EXPORT unsigned pk1_lev_inplace(void) { return INPLACE_NONE; }
+
+// ============================================================================
+// add_sed for callers that cannot allocate device memory.
+//
+// Some callers of this library may not call cudaMalloc: code running while
+// a CUDA graph is being captured, embedders whose device memory is all
+// handed out by their own pool, or runtimes that forbid allocation after
+// start-up.  For them gcvl_add_sed_noalloc runs the same segmented +-scan as
+// add_sed but keeps its look-back scratch in the fixed array below instead
+// of a caller scratch vector or the library workspace, and it allocates
+// nothing: no cudaMalloc, cudaFree or other allocating call, and it does not
+// run the library's own first-use set-up (which allocates).
+//
+// The array holds the scratch of at most GCVL_NOALLOC_MAX_N elements
+// (2^28) and stays allocated on every GPU that loads the library until the
+// process exits.  All calls share it and it keeps the last call's contents;
+// each call clears the part that must start at zero.  Calls that overlap on
+// the GPU race on it: issue them on one stream, or order them.
+// ============================================================================
+constexpr long kNoallocMaxN = 1L << 28;
+constexpr size_t kNoallocTiles = (size_t)(kNoallocMaxN / tile_elems<double>());  // smallest tiling
+constexpr size_t kNoallocBytes = 256 + ((kNoallocTiles * 4 + 255) / 256) * 256 + 2 * (((kNoallocTiles * 8) + 255) / 256) * 256;
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocBytes];
+static __device__ unsigned g_noalloc_status;
+
+// Device addresses of the array and of its status word, looked up once per
+// device (with that device current) on the first call made on it.
+static void *g_noalloc_ptr[128];
+static unsigned *g_noalloc_status_ptr[128];
+
+GCVL_EXPORT int gcvl_add_sed_noalloc(vec_p d, vec_p s, vec_p sd, int n, int m) {
+  using namespace gcvl;
+  if (n < 0 || m < 0 || (long)n > kNoallocMaxN) {
+    set_error(GCVL_ERR_RANGE, "gcvl_add_sed_noalloc: n = %d outside [0, %ld]", n, kNoallocMaxN);
+    return GCVL_ERR_RANGE;
+  }
+  if (n == 0) return GCVL_OK;
+  int dev = 0;
+  if (!GCVL_CK(cudaGetDevice(&dev))) return GCVL_ERR_CUDA;
+  if (dev < 0 || dev >= 128) { set_error(GCVL_ERR_RANGE, "gcvl_add_sed_noalloc: device %d", dev); return GCVL_ERR_RANGE; }
+  if (!g_noalloc_ptr[dev]) {
+    void *p = nullptr, *q = nullptr;
+    cudaError_t e1 = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    cudaError_t e2 = cudaGetSymbolAddress(&q, g_noalloc_status);
+    if (e1 != cudaSuccess || e2 != cudaSuccess) {
+      set_error(GCVL_ERR_CUDA, "gcvl_add_sed_noalloc: cudaGetSymbolAddress: %s",
+                cudaGetErrorString(e1 != cudaSuccess ? e1 : e2));
+      return GCVL_ERR_CUDA;
+    }
+    g_noalloc_ptr[dev] = p;
+    g_noalloc_status_ptr[dev] = (unsigned *)q;
+  }
+  State &S = st();
+  cudaStream_t strm = S.ready ? S.stream : (cudaStream_t)0;
+  void *mem = g_noalloc_ptr[dev];
+  const bool seg = (m != 1) && sd != nullptr;
+  const double *in = (const double *)s;
+  double *out = (double *)d;
+  const long rows = (long)n / row_items<double>();
+  CUtensorMap tin, tout;
+  const bool tma = !getenv("GCVL_NO_TMA") && rows >= 1 && !((size_t)in & 15) && !((size_t)out & 15) &&
+                   tma_map<double>(&tin, in, rows) && tma_map<double>(&tout, out, rows);
+  const int tiles = tma ? ceil_div(n, (long)TT * row_items<double>()) : ceil_div(n, tile_elems<double>());
+  if (lookback_bytes(tiles) > kNoallocBytes) {
+    set_error(GCVL_ERR_RANGE, "gcvl_add_sed_noalloc: %d tiles exceed the fixed scratch", tiles);
+    return GCVL_ERR_RANGE;
+  }
+  if (!GCVL_CK(cudaMemsetAsync(mem, 0, lookback_clear_bytes(tiles), strm))) return GCVL_ERR_CUDA;
+  if (tma) {
+    TArgs<double> a;
+    a.out = out; a.in = in; a.n = n; a.rows = rows;
+    a.sv = seg ? seg_view(sd, n, m) : SegView{nullptr, nullptr, nullptr, n, 1};
+    a.lb = lookback_carve(mem, tiles);
+    a.status = g_noalloc_status_ptr[dev];
+    a.spin_limit = S.spin_limit;
+    if (seg) k_scan_tma<AddD, M_SCAN, true><<<tiles, TT, tma_smem<double>(), strm>>>(tin, tout, a);
+    else k_scan_tma<AddD, M_SCAN, false><<<tiles, TT, tma_smem<double>(), strm>>>(tin, tout, a);
+  } else {
+    ScanArgs<double> a;
+    a.out = out; a.in = in; a.out2 = nullptr; a.n = n;
+    a.sv = seg ? seg_view(sd, n, m) : SegView{nullptr, nullptr, nullptr, n, 1};
+    a.lb = lookback_carve(mem, tiles);
+    a.status = g_noalloc_status_ptr[dev];
+    a.spin_limit = S.spin_limit;
+    a.count_flags = 0;
+    if (seg) k_scan<AddD, M_SCAN, true><<<tiles, Tiling<double>::BLOCK, 0, strm>>>(a);
+    else k_scan<AddD, M_SCAN, false><<<tiles, Tiling<double>::BLOCK, 0, strm>>>(a);
+  }
+  launch_check("gcvl_add_sed_noalloc");
+  return cudaPeekAtLastError() == cudaSuccess ? GCVL_OK : GCVL_ERR_CUDA;
+}
+
+GCVL_EXPORT long gcvl_add_sed_noalloc_max_n(void) { return kNoallocMaxN; }
