@@ -415,7 +415,9 @@ def gpu_arm(a):
 
 # ------------------------------------------------------ reference arm ---
 def reference_arm(a):
-    world, rank, local, pg = dist()
+    # rank 0 alone times the CPU implementation; other ranks exit at once
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     from neslgpu_gb300 import workloads as W
