@@ -185,32 +185,42 @@ template <class T> __device__ __forceinline__ T ld_relaxed(const T *p) {
 }
 
 // --------------------------------------------------- segment descriptor ---
-// Device layout of a segment descriptor (all int32, in one vec_p of
+// Device layout of a segment descriptor (32-bit words, in one vec_p of
 // siz_fos(n, m) units):
 //   [0, m)                    segment lengths (what len_fos returns)
 //   [L0, L0 + m + 1)          offsets: exclusive scan of the lengths, then n
 //   [L1, L1 + ng + 1)         granule table: for granule g (elements
 //                             g*kGranule...), the segment that holds element
 //                             g*kGranule; entry ng holds m
-// with L0 = align4(m), L1 = L0 + align4(m + 1), ng = ceil(n / kGranule).
+//   [L2, L2 + nb)             head bitmap: bit k set when element k starts a
+//                             (non-empty) segment; padded with zero words to a
+//                             multiple of 256 words
+// with L0 = align4(m), L1 = L0 + align4(m + 1), L2 = L1 + align4(ng + 1),
+// ng = ceil(n / kGranule), nb = align256(ceil(n / 32)).
 constexpr int kGranule = 64;
 struct SegView {
   const int *len;
   const int *off;
   const int *gran;
+  const unsigned *bits;
   int n, m;
 };
 __host__ __device__ inline long segdes_off_words(int m) { return ((long)m + 3) & ~3L; }
 __host__ __device__ inline long segdes_gran_words(int m) {
   return segdes_off_words(m) + (((long)m + 1 + 3) & ~3L);
 }
-__host__ __device__ inline long segdes_total_words(int n, int m) {
+__host__ __device__ inline long segdes_bits_words(int n, int m) {
   long ng = ((long)n + kGranule - 1) / kGranule;
   return segdes_gran_words(m) + ((ng + 1 + 3) & ~3L);
 }
+__host__ __device__ inline long segdes_nbits_words(int n) { return ((((long)n + 31) / 32) + 255) & ~255L; }
+__host__ __device__ inline long segdes_total_words(int n, int m) {
+  return segdes_bits_words(n, m) + segdes_nbits_words(n);
+}
 inline SegView seg_view(vec_p sd, int n, int m) {
   const int *b = (const int *)sd;
-  return SegView{b, b + segdes_off_words(m), b + segdes_gran_words(m), n, m};
+  return SegView{b, b + segdes_off_words(m), b + segdes_gran_words(m),
+                 (const unsigned *)(b + segdes_bits_words(n, m)), n, m};
 }
 
 // Segment holding element k (0 <= k < n): the largest s with off[s] <= k.

@@ -308,7 +308,7 @@ void rank_impl(vec_p d, vec_p s, vec_p sd, int n, int m, vec_p scratch, int is_d
 
   RankPrep p;
   p.src = s; p.n = n; p.is_double = is_double; p.up = up; p.seg = seg ? 1 : 0;
-  p.sv = seg ? seg_view(sd, n, m) : SegView{nullptr, nullptr, nullptr, n, 1};
+  p.sv = seg ? seg_view(sd, n, m) : SegView{nullptr, nullptr, nullptr, nullptr, n, 1};
   p.key = mem + L.key_a; p.idx = (unsigned *)(mem + L.idx_a);
   p.aux = seg ? (unsigned *)(mem + L.aux_a) : nullptr;
   p.hist = hist; p.key_passes = key_passes; p.seg_passes = seg_passes;

@@ -376,47 +376,54 @@ __global__ void __launch_bounds__(TT) k_scan_tma(const __grid_constant__ CUtenso
   __shared__ int s_wf[NW], s_wpf[NW];
   __shared__ T s_wv[NW], s_wpv[NW];
   __shared__ T s_prefix;
-  __shared__ unsigned s_tile;
-  __shared__ int s_sfirst, s_slast;
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  if (tid == 0) {
-    s_tile = atomicAdd(a.lb.counter, 1u);
-    mbar_init(&bar, 1);
-    fence_mbar_init();
-  }
-  __syncthreads();
-  const int tile = (int)s_tile;
+  // Tiles are taken in block order; blocks are dispatched in index order, so
+  // every predecessor a tile waits for is running or done (and the waits are
+  // bounded regardless).
+  const int tile = blockIdx.x;
   const long base = (long)tile * TILE;
   const int valid = (int)min((long)TILE, (long)a.n - base);
   if (tid == 0) {
+    mbar_init(&bar, 1);
+    fence_mbar_init();
     mbar_arrive_expect_tx(&bar, TILE * (unsigned)sizeof(T));
     tma_load_2d(tile_b, &tin, &bar, 0, tile * TT);
   }
-  if (SEG) {
-    if (tid == 0) s_sfirst = seg_of(a.sv, (int)base);
-    if (tid == 32) s_slast = seg_of(a.sv, (int)base + valid - 1);
+  const int k0 = (int)base + tid * ITEMS;
+  const int cnt = max(0, min(ITEMS, a.n - k0));
+  // segment heads of this thread's row, from the descriptor's head bitmap
+  unsigned heads = 0;
+  if (cnt > 0) {
+    if (SEG) {
+      const unsigned w = __ldg(a.sv.bits + (k0 >> 5));
+      heads = (ITEMS == 32) ? w : ((w >> (k0 & 31)) & ((1u << ITEMS) - 1u));
+      if (cnt < ITEMS) heads &= (1u << cnt) - 1u;
+    } else {
+      heads = (k0 == 0) ? 1u : 0u;
+    }
   }
-  __syncthreads();
+  // reductions also need segment numbers: a window of offsets whose bounds
+  // come straight from the granule table (tiles start on granule boundaries)
   int W = 0, sf = 0;
-  if (SEG) {
-    sf = s_sfirst;
-    W = s_slast - sf + 2;
+  if (SEG && MODE == M_REDUCE) {
+    sf = __ldg(a.sv.gran + base / kGranule);
+    const long e = base + valid;
+    const int sl = (e >= a.n) ? a.sv.m - 1 : __ldg(a.sv.gran + e / kGranule);
+    W = sl - sf + 2;
     if (W <= WMAX)
       for (int i = tid; i < W; i += TT) win[i] = __ldg(a.sv.off + sf + i);
   }
+  __syncthreads();  // barrier initialised; window loaded
   {
     int it = 0;
     while (!mbar_try_wait(&bar, 0)) {
       if (++it >= a.spin_limit) { atomicOr(a.status, DEV_TIMEOUT); break; }
     }
   }
-  __syncthreads();
   const OffWin off{win, a.sv.off, sf, (SEG && W <= WMAX) ? W : 0};
 
   // this thread's row
-  const int k0 = (int)base + tid * ITEMS;
-  const int cnt = max(0, min(ITEMS, a.n - k0));
   const long grow = (long)tile * TT + tid;
   T x[ITEMS];
   if (grow < a.rows) {
@@ -429,32 +436,22 @@ __global__ void __launch_bounds__(TT) k_scan_tma(const __grid_constant__ CUtenso
 #pragma unroll
     for (int i = 0; i < ITEMS; i++) x[i] = (i < cnt) ? a.in[k0 + i] : Op::ident();
   }
-
-  // segment heads of the row
-  unsigned heads = 0;
+  if constexpr (std::is_same<Op, CountB>::value) {
+#pragma unroll
+    for (int i = 0; i < ITEMS; i++) x[i] = x[i] != 0;  // pk1_lev counts true flags
+  }
+  // segment holding k0 (reductions): the last window entry <= k0
   int s0 = 0;
-  if (cnt > 0) {
-    if (SEG) {
-      if (W <= WMAX) {
-        int lo = 0, hi = W - 2;  // window index of the segment holding k0
-        while (lo < hi) {
-          int mid = (lo + hi + 1) >> 1;
-          if (win[mid] <= k0) lo = mid; else hi = mid - 1;
-        }
-        s0 = sf + lo;
-        if (win[lo] == k0) heads = 1u;
-        int j = lo, nxt = win[j + 1];
-        while (nxt < k0 + cnt) {
-          heads |= 1u << (nxt - k0);
-          ++j;
-          while (win[j + 1] == nxt) ++j;
-          nxt = win[j + 1];
-        }
-      } else {
-        heads = head_bits<ITEMS>(a.sv, k0, cnt, s0);
+  if (SEG && MODE == M_REDUCE && cnt > 0) {
+    if (W <= WMAX) {
+      int lo = 0, hi = W - 2;
+      while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (win[mid] <= k0) lo = mid; else hi = mid - 1;
       }
+      s0 = sf + lo;
     } else {
-      heads = (k0 == 0) ? 1u : 0u;
+      s0 = seg_of(a.sv, k0);
     }
   }
 
@@ -673,7 +670,7 @@ bool run_scan_tma(typename Op::T *out, const typename Op::T *in, vec_p sd, int n
   if (!mem) return true;
   TArgs<T> a;
   a.out = out; a.in = in; a.n = n; a.rows = rows;
-  a.sv = SEG ? seg_view(sd, n, m) : SegView{nullptr, nullptr, nullptr, n, 1};
+  a.sv = SEG ? seg_view(sd, n, m) : SegView{nullptr, nullptr, nullptr, nullptr, n, 1};
   a.lb = lookback_carve(mem, tiles);
   a.status = S.d_status;
   a.spin_limit = S.spin_limit;
@@ -705,14 +702,15 @@ void run_scan(typename Op::T *out, const typename Op::T *in, typename Op::T *out
   State &S = st();
   if (n <= 0) return;
   if constexpr (MODE == M_SCAN || MODE == M_REDUCE) {
-    if (!count_flags && run_scan_tma<Op, MODE, SEG>(out, in, sd, n, m, scratch, name)) return;
+    const bool tma_ok = !count_flags || std::is_same<Op, CountB>::value;
+    if (tma_ok && run_scan_tma<Op, MODE, SEG>(out, in, sd, n, m, scratch, name)) return;
   }
   const int tiles = ceil_div(n, tile_elems<T>());
   void *mem = scratch_or_work(scratch, lookback_bytes(tiles));
   if (!mem) return;
   ScanArgs<T> a;
   a.out = out; a.in = in; a.out2 = out2; a.n = n;
-  a.sv = SEG ? seg_view(sd, n, m) : SegView{nullptr, nullptr, nullptr, n, 1};
+  a.sv = SEG ? seg_view(sd, n, m) : SegView{nullptr, nullptr, nullptr, nullptr, n, 1};
   a.lb = lookback_carve(mem, tiles);
   a.status = S.d_status;
   a.spin_limit = S.spin_limit;
@@ -864,6 +862,14 @@ __global__ void k_granules(SegView sv, int *gran, int ng) {
   gran[g] = lo;
 }
 
+// Head bitmap: one bit per element, set where a non-empty segment starts.
+__global__ void k_headbits(SegView sv, unsigned *bits) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= sv.m) return;
+  const int o = sv.off[s];
+  if (sv.off[s + 1] > o) atomicOr(bits + (o >> 5), 1u << (o & 31));
+}
+
 void make_segdes(vec_p sd, vec_p l, int n, int m, vec_p scratch) {
   ensure_init();
   State &S = st();
@@ -885,6 +891,12 @@ void make_segdes(vec_p sd, vec_p l, int n, int m, vec_p scratch) {
   if (m <= 0) ng = 0;
   k_granules<<<ceil_div(ng + 1, 256), 256, 0, S.stream>>>(sv, gran, ng);
   launch_check("k_granules");
+  unsigned *bits = (unsigned *)(base + segdes_bits_words(n, m));
+  GCVL_CK(cudaMemsetAsync(bits, 0, (size_t)segdes_nbits_words(n) * 4, S.stream));
+  if (m > 0) {
+    k_headbits<<<ceil_div(m, 256), 256, 0, S.stream>>>(sv, bits);
+    launch_check("k_headbits");
+  }
 }
 
 }  // namespace gcvl
@@ -1031,7 +1043,7 @@ GCVL_EXPORT int gcvl_add_sed_noalloc(vec_p d, vec_p s, vec_p sd, int n, int m) {
   if (tma) {
     TArgs<double> a;
     a.out = out; a.in = in; a.n = n; a.rows = rows;
-    a.sv = seg ? seg_view(sd, n, m) : SegView{nullptr, nullptr, nullptr, n, 1};
+    a.sv = seg ? seg_view(sd, n, m) : SegView{nullptr, nullptr, nullptr, nullptr, n, 1};
     a.lb = lookback_carve(mem, tiles);
     a.status = g_noalloc_status_ptr[dev];
     a.spin_limit = S.spin_limit;
@@ -1040,7 +1052,7 @@ GCVL_EXPORT int gcvl_add_sed_noalloc(vec_p d, vec_p s, vec_p sd, int n, int m) {
   } else {
     ScanArgs<double> a;
     a.out = out; a.in = in; a.out2 = nullptr; a.n = n;
-    a.sv = seg ? seg_view(sd, n, m) : SegView{nullptr, nullptr, nullptr, n, 1};
+    a.sv = seg ? seg_view(sd, n, m) : SegView{nullptr, nullptr, nullptr, nullptr, n, 1};
     a.lb = lookback_carve(mem, tiles);
     a.status = g_noalloc_status_ptr[dev];
     a.spin_limit = S.spin_limit;

@@ -44,6 +44,32 @@ __device__ __forceinline__ void tma_store_2d(const CUtensorMap *map, const void 
                ::"l"(map), "r"(smem_addr(src)), "r"(x), "r"(y)
                : "memory");
 }
+// 1-D bulk copy global -> shared (16-byte aligned addresses, size % 16 == 0).
+__device__ __forceinline__ void bulk_load_1d(void *dst, const void *src, unsigned bytes,
+                                             unsigned long long *bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+      ::"r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(unsigned long long *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+// Bounded wait for the completion of phase `parity`; false on timeout.
+__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned parity, int limit) {
+  int it = 0;
+  while (!mbar_try_wait(bar, parity)) {
+    if (++it >= limit) return false;
+  }
+  return true;
+}
+__device__ __forceinline__ void bulk_wait_read_1() {
+  asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
+}
+// Barrier among the first `n` threads of the CTA (the consumer warps).
+__device__ __forceinline__ void named_sync(int id, int n) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory");
+}
 __device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void bulk_wait_read_all() {
   asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
