@@ -198,12 +198,17 @@ def primitive_suite(g, n, hbm):
     c.c2v_fuz(lv, lens.ctypes.data, m, None)
     sd = g.alloc(c.siz_fos(n, m))
     scr = g.alloc(max(c.mke_fov_scratch(n, m), c.add_sez_scratch(n, m), c.max_rez_scratch(n, m),
-                      c.pk2_luz_scratch(n), c.rku_luz_scratch(n), c.pk1_lev_scratch(n, m)))
+                      c.pk2_luz_scratch(n), c.rku_luz_scratch(n), c.rku_lez_scratch(n, m),
+                      c.pk1_lev_scratch(n, m)))
     c.mke_fov(sd, lv, n, m, scr)
     # a uniform random permutation: the rank of uniform random keys
     c.rku_luz(ix, yi, n, scr)
     red = g.alloc(c.siz_foz(m))
     cnt = c.pk1_luv(fl, n, scr)
+    # indices local to each segment for the segmented gather: rank of random
+    # keys within segments (a random permutation of every segment)
+    ix_seg = g.alloc(c.siz_foz(n))
+    c.rku_lez(ix_seg, yi, sd, n, m, scr)
 
     def rec(name, fn, bytes_per_elem, extra=0.0):
         t = timed(g, fn)
@@ -217,6 +222,10 @@ def primitive_suite(g, n, hbm):
     rec("max_rez", lambda: c.max_rez(red, xi, sd, n, m, scr), 4, 8.0 * m)
     rec("pk1_lev+pk2_lez (pack)", lambda: (c.pk1_lev(red, fl, sd, n, m, scr),
                                            c.pk2_lez(dz, xi, fl, sd, n, m, sd, cnt, m, scr)), 8, 4.0 * cnt + 8.0 * m)
+    rec("pk1_lev", lambda: c.pk1_lev(red, fl, sd, n, m, scr), 4, 8.0 * m)
+    rec("pk2_lez", lambda: c.pk2_lez(dz, xi, fl, sd, n, m, sd, cnt, m, scr), 8, 4.0 * cnt)
+    rec("dis_vez", lambda: c.dis_vez(dz, red, sd, n, m, None), 4, 8.0 * m)
+    rec("bck_pez (segmented gather)", lambda: c.bck_pez(dz, xi, ix_seg, sd, n, m, sd, n, m, None), 12, 8.0 * m)
     rec("smp_puz (permute)", lambda: c.smp_puz(dz, xi, ix, n, None), 12)
     rec("bck_puz (back-permute)", lambda: c.bck_puz(dz, xi, ix, n, n, None), 12)
     rec("add_wuz", lambda: c.add_wuz(dz, xi, yi, n, None), 12)
@@ -227,7 +236,7 @@ def primitive_suite(g, n, hbm):
                              "frac_io_floor": round(io * n / (t * 1e-3) / 1e9 / hbm, 3),
                              "frac_pass_traffic_76B": round(passes * n / (t * 1e-3) / 1e9 / hbm, 3)}
     g.check(c)
-    for p in (xi, yi, dz, fl, ix, lv, sd, scr, red):
+    for p in (xi, yi, dz, fl, ix, ix_seg, lv, sd, scr, red):
         c.fre_fov(p)
     return out
 

@@ -238,39 +238,113 @@ __device__ __forceinline__ int seg_of(const SegView &v, int k) {
   return lo;
 }
 
-// --------------------------------------------------- tile status arrays ---
+// --------------------------------------------------- tile status words ---
 // Decoupled look-back state for one launch, carved out of scratch:
-//   counter (u32, dynamic tile ticket), flags[tiles] (u32),
-//   agg[tiles] (T, 8-byte slots), inc[tiles] (T, 8-byte slots).
-// Only counter and flags need clearing before a launch.
+//   counter (u32, dynamic tile ticket), then one 16-byte word per tile:
+//   {status, value bits}, written with one 128-bit store and read with one
+//   128-bit load.  The word is self-contained -- no other data is read on the
+//   strength of its status -- so relaxed ordering suffices, and a warp's
+//   loads of many predecessors' words are all in flight at once (acquire
+//   loads would each wait for the one before).
+// The whole area is cleared before a launch.
 enum : unsigned { TS_EMPTY = 0, TS_AGG = 1, TS_INC = 2 };
 struct LookbackMem {
   unsigned *counter;
-  unsigned *flags;
-  unsigned long long *agg;
-  unsigned long long *inc;
+  ulonglong2 *word;
 };
-inline size_t lookback_bytes(int tiles) {
-  return 256 + align_up((size_t)tiles * 4, 256) + 2 * align_up((size_t)tiles * 8, 256);
-}
-inline size_t lookback_clear_bytes(int tiles) { return 256 + align_up((size_t)tiles * 4, 256); }
+// The area is placed at the first 256-byte boundary of the scratch: the
+// 128-bit status accesses need 16-byte alignment, and a caller's scratch
+// vector (sub-allocated in 8-byte units) need not have it.
+inline size_t lookback_bytes(int tiles) { return 512 + align_up((size_t)tiles * 16, 256); }
+inline size_t lookback_clear_bytes(int tiles) { return lookback_bytes(tiles); }
 inline LookbackMem lookback_carve(void *base, int tiles) {
-  char *p = (char *)base;
-  LookbackMem L;
-  L.counter = (unsigned *)p;
-  L.flags = (unsigned *)(p + 256);
-  L.agg = (unsigned long long *)(p + 256 + align_up((size_t)tiles * 4, 256));
-  L.inc = (unsigned long long *)((char *)L.agg + align_up((size_t)tiles * 8, 256));
-  return L;
+  (void)tiles;
+  char *p = (char *)align_up((size_t)base, 256);
+  return LookbackMem{(unsigned *)p, (ulonglong2 *)(p + 256)};
 }
 // scratch units (8 bytes) needed by a look-back launch of `tiles` tiles
 inline int lookback_units(int tiles) { return (int)((lookback_bytes(tiles) + 7) / 8); }
+
+__device__ __forceinline__ void lb_publish(ulonglong2 *w, unsigned long long status, unsigned long long bits) {
+  asm volatile("{\n .reg .b128 t;\n mov.b128 t, {%1, %2};\n st.relaxed.gpu.global.b128 [%0], t;\n}"
+               ::"l"(w), "l"(status), "l"(bits) : "memory");
+}
+__device__ __forceinline__ void lb_read(const ulonglong2 *w, unsigned long long &status,
+                                        unsigned long long &bits) {
+  asm volatile("{\n .reg .b128 t;\n ld.relaxed.gpu.global.b128 t, [%2];\n mov.b128 {%0, %1}, t;\n}"
+               : "=l"(status), "=l"(bits) : "l"(w) : "memory");
+}
 
 template <class T> __device__ __forceinline__ unsigned long long to_bits(T v) {
   unsigned long long b = 0; memcpy(&b, &v, sizeof(T)); return b;
 }
 template <class T> __device__ __forceinline__ T from_bits(unsigned long long b) {
   T v; memcpy(&v, &b, sizeof(T)); return v;
+}
+
+// Exclusive prefix of `tile` over the words earlier tiles published, run by
+// one whole warp.  Each step covers 32 * LB_K predecessors (LB_K words per
+// lane, loaded together), combined in element order, until an inclusive word
+// is found: with a thousand tiles in flight most predecessors have published
+// only their aggregate, and wide steps keep the walk to one or two round
+// trips.  Every wait is bounded by spin_limit.
+constexpr int LB_K = 4;
+template <class Op>
+__device__ __forceinline__ typename Op::T lookback_prefix(const ulonglong2 *words, int tile,
+                                                          unsigned *status, int spin_limit) {
+  typedef typename Op::T T;
+  const int lane = threadIdx.x & 31;
+  T P = Op::ident();
+  int pred = tile - 1;
+  while (true) {
+    // lane l holds predecessors pred - l*LB_K - j, j = 0 (nearest) .. LB_K-1
+    unsigned long long stt[LB_K], bits[LB_K];
+#pragma unroll
+    for (int j = 0; j < LB_K; j++) {
+      const int t = pred - lane * LB_K - j;
+      stt[j] = TS_INC;
+      bits[j] = to_bits<T>(Op::ident());
+      if (t >= 0) lb_read(words + t, stt[j], bits[j]);
+    }
+#pragma unroll
+    for (int j = 0; j < LB_K; j++) {
+      const int t = pred - lane * LB_K - j;
+      int it = 0;
+      while (stt[j] == TS_EMPTY) {
+        if (++it >= spin_limit) {
+          atomicOr(status, DEV_TIMEOUT);
+          stt[j] = TS_INC;
+          bits[j] = to_bits<T>(Op::ident());
+          break;
+        }
+        __nanosleep(32);
+        lb_read(words + t, stt[j], bits[j]);
+      }
+    }
+    // nearest inclusive word of this lane, and the lane's fold from there
+    // (or from its farthest word) to its nearest, in element order
+    int jinc = LB_K;
+#pragma unroll
+    for (int j = LB_K - 1; j >= 0; j--)
+      if (stt[j] == TS_INC) jinc = j;
+    T val = Op::ident();
+#pragma unroll
+    for (int j = LB_K - 1; j >= 0; j--)
+      if (j <= jinc || jinc == LB_K) val = Op::apply(val, from_bits<T>(bits[j]));
+    const unsigned incm = __ballot_sync(0xffffffffu, jinc < LB_K);
+    const int stop = incm ? __ffs(incm) - 1 : 31;
+    if (lane > stop) val = Op::ident();
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      T o = shfl_down(val, d);
+      if (lane + d < 32) val = Op::apply(o, val);
+    }
+    val = shfl_idx(val, 0);
+    P = Op::apply(val, P);
+    if (incm) break;
+    pred -= 32 * LB_K;
+  }
+  return P;
 }
 
 }  // namespace gcvl

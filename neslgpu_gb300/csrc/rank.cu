@@ -25,6 +25,7 @@ namespace gcvl {
 constexpr int RK_BLOCK = 256, RK_ITEMS = 16, RK_TILE = RK_BLOCK * RK_ITEMS;
 constexpr int RK_WARPS = RK_BLOCK / 32;
 constexpr int RK_MAXPASS = 12;
+constexpr int RK_LB = 8;  // predecessors read per look-back round trip
 enum : unsigned long long { RK_AGG = 1ULL << 62, RK_INC = 2ULL << 62, RK_MASK = (1ULL << 62) - 1 };
 
 struct RankPrep {
@@ -168,28 +169,41 @@ __global__ void __launch_bounds__(RK_BLOCK) k_rank_pass(PassArgs<K> a) {
   // publish this tile's digit count, then look back for earlier tiles'
   unsigned long long *st = a.state + (long)tile * 256 + dd;
   if (tile == 0) {
-    asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(st), "l"(RK_INC | tot) : "memory");
+    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(st), "l"(RK_INC | tot) : "memory");
   } else {
-    asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(st), "l"(RK_AGG | tot) : "memory");
+    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(st), "l"(RK_AGG | tot) : "memory");
   }
+  // look back for this digit: RK_LB predecessors per round trip, nearest
+  // first, until an inclusive count is found (bounded waits).  Each status
+  // word is self-contained, so relaxed loads suffice and all RK_LB are in
+  // flight together.
   unsigned long long prefix = 0;
   if (tile > 0) {
-    long t = tile - 1;
-    while (t >= 0) {
-      const unsigned long long *p = a.state + t * 256 + dd;
-      unsigned long long w;
-      int it = 0;
-      do {
-        asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(w) : "l"(p) : "memory");
-        if (w != 0) break;
-        __nanosleep(32);
-      } while (++it < a.spin_limit);
-      if (w == 0) { atomicOr(a.status, DEV_TIMEOUT); break; }
-      prefix += w & RK_MASK;
-      if (w & RK_INC) break;
-      --t;
+    long t0 = tile - 1;
+    bool done = false;
+    while (!done && t0 >= 0) {
+      unsigned long long w[RK_LB];
+#pragma unroll
+      for (int j = 0; j < RK_LB; j++) {
+        w[j] = RK_INC;  // beyond tile 0: an inclusive zero
+        if (t0 - j >= 0)
+          asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(w[j]) : "l"(a.state + (t0 - j) * 256 + dd) : "memory");
+      }
+#pragma unroll
+      for (int j = 0; j < RK_LB; j++) {
+        if (done) break;
+        int it = 0;
+        while (w[j] == 0) {
+          if (++it >= a.spin_limit) { atomicOr(a.status, DEV_TIMEOUT); w[j] = RK_INC; break; }
+          __nanosleep(32);
+          asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(w[j]) : "l"(a.state + (t0 - j) * 256 + dd) : "memory");
+        }
+        prefix += w[j] & RK_MASK;
+        if (w[j] & RK_INC) done = true;
+      }
+      t0 -= RK_LB;
     }
-    asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(st), "l"(RK_INC | (prefix + tot)) : "memory");
+    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(st), "l"(RK_INC | (prefix + tot)) : "memory");
   }
   // exclusive scan of tile counts over the digits -> local offsets
   {

@@ -178,50 +178,11 @@ k_scan(ScanArgs<typename Op::T> a) {
     // thread 0 holds element `base`: its head bit says whether the tile
     // starts a segment (then no carry from earlier tiles is needed)
     const bool first_head = shfl_idx((int)(heads & 1u), 0) != 0;
-    if (lane == 0) {
-      if (tile == 0 || af) {
-        st_relaxed(a.lb.inc + tile, to_bits<T>(av));
-        st_release(a.lb.flags + tile, TS_INC);
-      } else {
-        st_relaxed(a.lb.agg + tile, to_bits<T>(av));
-        st_release(a.lb.flags + tile, TS_AGG);
-      }
-    }
+    if (lane == 0) lb_publish(a.lb.word + tile, (tile == 0 || af) ? TS_INC : TS_AGG, to_bits<T>(av));
     T P = Op::ident();
     if (tile > 0 && !first_head) {
-      int pred = tile - 1;
-      while (true) {
-        int t = pred - lane;
-        unsigned fl = TS_INC;
-        T val = Op::ident();
-        if (t >= 0) {
-          int it = 0;
-          fl = ld_acquire(a.lb.flags + t);
-          while (fl == TS_EMPTY) {
-            if (++it >= a.spin_limit) break;
-            __nanosleep(32);
-            fl = ld_acquire(a.lb.flags + t);
-          }
-          if (fl == TS_EMPTY) { atomicOr(a.status, DEV_TIMEOUT); fl = TS_INC; }
-          else val = from_bits<T>(ld_relaxed(fl == TS_INC ? a.lb.inc + t : a.lb.agg + t));
-        }
-        unsigned incm = __ballot_sync(0xffffffffu, fl == TS_INC);
-        int stop = incm ? __ffs(incm) - 1 : 31;
-        if (lane > stop) val = Op::ident();
-#pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-          T o = shfl_down(val, d);
-          if (lane + d < 32) val = Op::apply(o, val);
-        }
-        val = shfl_idx(val, 0);
-        P = Op::apply(val, P);
-        if (incm) break;
-        pred -= 32;
-      }
-      if (lane == 0 && !af) {
-        st_relaxed(a.lb.inc + tile, to_bits<T>(Op::apply(P, av)));
-        st_release(a.lb.flags + tile, TS_INC);
-      }
+      P = lookback_prefix<Op>(a.lb.word, tile, a.status, a.spin_limit);
+      if (lane == 0 && !af) lb_publish(a.lb.word + tile, TS_INC, to_bits<T>(Op::apply(P, av)));
     }
     if (lane == 0) s_prefix = P;
   }
@@ -279,8 +240,11 @@ k_scan(ScanArgs<typename Op::T> a) {
 // GB300's narrow FP64 pipe free for the one add per element that an
 // exclusive scan output needs.
 // ============================================================================
-constexpr int TT = 256;    // threads per CTA = rows per tile
-constexpr int WMAX = 2048; // offsets window held in shared memory
+#ifndef GCVL_TT
+#define GCVL_TT 128
+#endif
+constexpr int TT = GCVL_TT;  // threads per CTA = rows per tile
+constexpr int WMAX = 1024;   // offsets window held in shared memory
 template <class T> constexpr int row_items() { return 128 / (int)sizeof(T); }
 
 template <class T> struct TArgs {
@@ -334,7 +298,7 @@ template <int ITEMS> struct Engine<AddD, ITEMS> {
         if (i >= from && i < cnt) tv = (i == from && tf) ? AddD::apply(0.0, x[i]) : AddD::apply(tv, x[i]);
       return;
     }
-    Fx128 acc{0ULL, 0ULL};
+    long long acc = 0;
 #pragma unroll
     for (int i = 0; i < ITEMS; i++)
       if (i >= from && i < cnt) fx_add(acc, (unsigned long long)__double_as_longlong(x[i]), emax);
@@ -356,7 +320,7 @@ __device__ __forceinline__ double fx_range(const double (&x)[ITEMS], int from, i
       if (i >= from && i < to) v = __dadd_rn(v, x[i]);
     return v;
   }
-  Fx128 acc{0ULL, 0ULL};
+  long long acc = 0;
 #pragma unroll
   for (int i = 0; i < ITEMS; i++)
     if (i >= from && i < to) fx_add(acc, (unsigned long long)__double_as_longlong(x[i]), emax);
@@ -364,7 +328,7 @@ __device__ __forceinline__ double fx_range(const double (&x)[ITEMS], int from, i
 }
 
 template <class Op, int MODE, bool SEG>
-__global__ void __launch_bounds__(TT) k_scan_tma(const __grid_constant__ CUtensorMap tin,
+__global__ void __launch_bounds__(TT, 768 / TT) k_scan_tma(const __grid_constant__ CUtensorMap tin,
                                                  const __grid_constant__ CUtensorMap tout,
                                                  TArgs<typename Op::T> a) {
   typedef typename Op::T T;
@@ -491,50 +455,11 @@ __global__ void __launch_bounds__(TT) k_scan_tma(const __grid_constant__ CUtenso
     const int af = shfl_idx(wf, NW - 1);
     const T av = shfl_idx(wv, NW - 1);
     const bool first_head = shfl_idx((int)(heads & 1u), 0) != 0;
-    if (lane == 0) {
-      if (tile == 0 || af) {
-        st_relaxed(a.lb.inc + tile, to_bits<T>(av));
-        st_release(a.lb.flags + tile, TS_INC);
-      } else {
-        st_relaxed(a.lb.agg + tile, to_bits<T>(av));
-        st_release(a.lb.flags + tile, TS_AGG);
-      }
-    }
+    if (lane == 0) lb_publish(a.lb.word + tile, (tile == 0 || af) ? TS_INC : TS_AGG, to_bits<T>(av));
     T P = Op::ident();
     if (tile > 0 && !first_head) {
-      int pred = tile - 1;
-      while (true) {
-        int t = pred - lane;
-        unsigned fl = TS_INC;
-        T val = Op::ident();
-        if (t >= 0) {
-          int it = 0;
-          fl = ld_acquire(a.lb.flags + t);
-          while (fl == TS_EMPTY) {
-            if (++it >= a.spin_limit) break;
-            __nanosleep(32);
-            fl = ld_acquire(a.lb.flags + t);
-          }
-          if (fl == TS_EMPTY) { atomicOr(a.status, DEV_TIMEOUT); fl = TS_INC; }
-          else val = from_bits<T>(ld_relaxed(fl == TS_INC ? a.lb.inc + t : a.lb.agg + t));
-        }
-        unsigned incm = __ballot_sync(0xffffffffu, fl == TS_INC);
-        int stop = incm ? __ffs(incm) - 1 : 31;
-        if (lane > stop) val = Op::ident();
-#pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-          T o = shfl_down(val, d);
-          if (lane + d < 32) val = Op::apply(o, val);
-        }
-        val = shfl_idx(val, 0);
-        P = Op::apply(val, P);
-        if (incm) break;
-        pred -= 32;
-      }
-      if (lane == 0 && !af) {
-        st_relaxed(a.lb.inc + tile, to_bits<T>(Op::apply(P, av)));
-        st_release(a.lb.flags + tile, TS_INC);
-      }
+      P = lookback_prefix<Op>(a.lb.word, tile, a.status, a.spin_limit);
+      if (lane == 0 && !af) lb_publish(a.lb.word + tile, TS_INC, to_bits<T>(Op::apply(P, av)));
     }
     if (lane == 0) s_prefix = P;
   }
@@ -986,14 +911,14 @@ GCVL_EXPORT unsigned pk1_lev_inplace(void) { return INPLACE_NONE; }
 // run the library's own first-use set-up (which allocates).
 //
 // The array holds the scratch of at most GCVL_NOALLOC_MAX_N elements
-// (2^28) and stays allocated on every GPU that loads the library until the
+// (2^28; about 2 MB) and stays allocated on every GPU that loads the library until the
 // process exits.  All calls share it and it keeps the last call's contents;
 // each call clears the part that must start at zero.  Calls that overlap on
 // the GPU race on it: issue them on one stream, or order them.
 // ============================================================================
 constexpr long kNoallocMaxN = 1L << 28;
 constexpr size_t kNoallocTiles = (size_t)(kNoallocMaxN / tile_elems<double>());  // smallest tiling
-constexpr size_t kNoallocBytes = 256 + ((kNoallocTiles * 4 + 255) / 256) * 256 + 2 * (((kNoallocTiles * 8) + 255) / 256) * 256;
+constexpr size_t kNoallocBytes = 512 + ((kNoallocTiles * 16 + 255) / 256) * 256;
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocBytes];
 static __device__ unsigned g_noalloc_status;
 

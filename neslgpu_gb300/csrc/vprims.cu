@@ -143,6 +143,14 @@ __global__ void __launch_bounds__(PBLOCK) k_pack(T *__restrict__ d, const T *__r
   const long base = (long)tile * PTILE;
   const int valid = (int)min((long)PTILE, (long)n - base);
 
+  // values: coalesced striped loads issued first, kept in registers until
+  // their ranks are known (so their latency overlaps the ranking)
+  T vals[PITEMS];
+#pragma unroll
+  for (int j = 0; j < PITEMS; j++) {
+    int e = j * PBLOCK + tid;
+    if (e < valid) vals[j] = __ldcs(s + base + e);
+  }
   // flags: coalesced striped loads, transposed to 16 consecutive per thread
   const int wbase = warp * 32 * PITEMS;
 #pragma unroll
@@ -183,41 +191,11 @@ __global__ void __launch_bounds__(PBLOCK) k_pack(T *__restrict__ d, const T *__r
 
   // decoupled look-back over tile counts (int add, no segments)
   if (warp == 0) {
-    if (lane == 0) {
-      if (tile == 0) { st_relaxed(lb.inc + tile, (unsigned long long)total); st_release(lb.flags + tile, TS_INC); }
-      else { st_relaxed(lb.agg + tile, (unsigned long long)total); st_release(lb.flags + tile, TS_AGG); }
-    }
-    long P = 0;
+    if (lane == 0) lb_publish(lb.word + tile, tile == 0 ? TS_INC : TS_AGG, (unsigned long long)(unsigned)total);
+    int P = 0;
     if (tile > 0) {
-      int pred = tile - 1;
-      while (true) {
-        int t = pred - lane;
-        unsigned fl = TS_INC;
-        long val = 0;
-        if (t >= 0) {
-          int it = 0;
-          fl = ld_acquire(lb.flags + t);
-          while (fl == TS_EMPTY) {
-            if (++it >= spin_limit) break;
-            __nanosleep(32);
-            fl = ld_acquire(lb.flags + t);
-          }
-          if (fl == TS_EMPTY) { atomicOr(status, DEV_TIMEOUT); fl = TS_INC; }
-          else val = (long)ld_relaxed(fl == TS_INC ? lb.inc + t : lb.agg + t);
-        }
-        unsigned incm = __ballot_sync(0xffffffffu, fl == TS_INC);
-        int stop = incm ? __ffs(incm) - 1 : 31;
-        if (lane > stop) val = 0;
-#pragma unroll
-        for (int dd = 16; dd > 0; dd >>= 1) val += shfl_down(val, dd);
-        P += shfl_idx(val, 0);
-        if (incm) break;
-        pred -= 32;
-      }
-      if (lane == 0) {
-        st_relaxed(lb.inc + tile, (unsigned long long)(P + total));
-        st_release(lb.flags + tile, TS_INC);
-      }
+      P = lookback_prefix<AddZ>(lb.word, tile, status, spin_limit);
+      if (lane == 0) lb_publish(lb.word + tile, TS_INC, (unsigned long long)(unsigned)(P + total));
     }
     if (lane == 0) { s_prefix = (int)P; s_count = total; }
   }
@@ -226,8 +204,8 @@ __global__ void __launch_bounds__(PBLOCK) k_pack(T *__restrict__ d, const T *__r
 #pragma unroll
   for (int j = 0; j < PITEMS; j++) {
     int e = j * PBLOCK + tid;
-    int rk = s_rank[e + e / PE];
-    if (rk >= 0) s_val[rk] = __ldcs(s + base + e);
+    int rk = e < valid ? s_rank[e + e / PE] : -1;
+    if (rk >= 0) s_val[rk] = vals[j];
   }
   __syncthreads();
   const long out0 = s_prefix;
