@@ -744,6 +744,27 @@ unsigned long long gcvl_launch_count(void);
  * depends only on (seed, i).  kind 0: int32 uniform over all values,
  * 1: float64 N(0,1), 2: cvl_bool Bernoulli(a), 3: int32 uniform in [0, b). */
 void gcvl_fill_random(vec_p d, long n, int kind, unsigned long long seed, double a, int b);
+/* CUDA graphs over library calls: calls issued between gcvl_graph_begin and
+ * gcvl_graph_end are captured from the library stream into one executable
+ * graph (returned) instead of running.  Captured calls must not synchronise
+ * (no *_ru*, ext_vu*, pk1_luv, c2v_fu*, v2c_fu*) and must be given scratch.
+ * gcvl_graph_launch replays it on the library stream. */
+int gcvl_graph_begin(void);
+void *gcvl_graph_end(void);
+int gcvl_graph_launch(void *graph);
+void gcvl_graph_destroy(void *graph);
+/* add_ruz with the sum left in device memory at d[0] (no synchronisation),
+ * for sequences captured in a graph. */
+void gcvl_add_ruz_dev(vec_p d, vec_p s, int len, vec_p scratch);
+int gcvl_add_ruz_dev_scratch(int len);
+/* The per-vector CVL call sequence of the batched benchmark (one MAKE_SEGDES,
+ * +_SCAN, DIST, >, PACK, DIST, RAND, BPERMUTE sequence per vector, with the
+ * PACK length read back to the host each time, as vinterp does).  Returns 0
+ * or a GCVL error code. */
+int gcvl_pipeline_percall(int is_double, vec_p x, const int *seg_lens_host, const int *nseg_of,
+                          const int *len_of, int nvec, vec_p y, vec_p f, vec_p p, vec_p newlens,
+                          vec_p bnd, vec_p idx, vec_p g, vec_p zeros, vec_p lens_dev, vec_p sd,
+                          vec_p sd2, vec_p work, unsigned seed);
 /* Segmented exclusive +-scan of float64 (add_sed) that allocates nothing.
  * No counterpart in the reference.  For callers that may not allocate device
  * memory -- code running during CUDA graph capture, embedders whose device

@@ -327,10 +327,17 @@ __device__ __forceinline__ double fx_range(const double (&x)[ITEMS], int from, i
   return fx_to_double(acc, emax);
 }
 
+// The CTA has TT compute threads (one 128-byte row each) plus one look-back
+// warp.  The look-back warp issues the tile's TMA load and at once starts
+// collecting the carry from earlier tiles, while the compute warps fold their
+// rows: the carry's round trips overlap the load and the fold instead of
+// following them.  The compute warps publish the tile aggregate as soon as it
+// exists and meet the look-back warp only when they need the carry.
+constexpr int TB_LB = TT + 32;  // threads per CTA
 template <class Op, int MODE, bool SEG>
-__global__ void __launch_bounds__(TT, 768 / TT) k_scan_tma(const __grid_constant__ CUtensorMap tin,
-                                                 const __grid_constant__ CUtensorMap tout,
-                                                 TArgs<typename Op::T> a) {
+__global__ void __launch_bounds__(TB_LB, 5) k_scan_tma(const __grid_constant__ CUtensorMap tin,
+                                                     const __grid_constant__ CUtensorMap tout,
+                                                     TArgs<typename Op::T> a) {
   typedef typename Op::T T;
   constexpr int ITEMS = row_items<T>(), TILE = TT * ITEMS, NW = TT / 32;
   extern __shared__ unsigned char dyn_smem[];
@@ -339,7 +346,8 @@ __global__ void __launch_bounds__(TT, 768 / TT) k_scan_tma(const __grid_constant
   __shared__ unsigned long long bar;
   __shared__ int s_wf[NW], s_wpf[NW];
   __shared__ T s_wv[NW], s_wpv[NW];
-  __shared__ T s_prefix;
+  __shared__ T s_prefix, s_av;
+  __shared__ int s_af;
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   // Tiles are taken in block order; blocks are dispatched in index order, so
@@ -348,15 +356,31 @@ __global__ void __launch_bounds__(TT, 768 / TT) k_scan_tma(const __grid_constant
   const int tile = blockIdx.x;
   const long base = (long)tile * TILE;
   const int valid = (int)min((long)TILE, (long)a.n - base);
-  if (tid == 0) {
+  if (tid == TT) {
     mbar_init(&bar, 1);
     fence_mbar_init();
     mbar_arrive_expect_tx(&bar, TILE * (unsigned)sizeof(T));
     tma_load_2d(tile_b, &tin, &bar, 0, tile * TT);
   }
+  __syncthreads();  // barrier initialised
+
+  if (warp == NW) {
+    // ------------------------------------------------------ look-back warp
+    bool first_head;
+    if (SEG) first_head = (__ldg(a.sv.bits + (base >> 5)) >> (base & 31)) & 1u;
+    else first_head = base == 0;
+    T P = Op::ident();
+    if (tile > 0 && !first_head) P = lookback_prefix<Op>(a.lb.word, tile, a.status, a.spin_limit);
+    if (lane == 0) s_prefix = P;
+    named_sync(1, TB_LB);  // carry ready / tile aggregate ready
+    if (lane == 0 && tile > 0 && !first_head && !s_af)
+      lb_publish(a.lb.word + tile, TS_INC, to_bits<T>(Op::apply(P, s_av)));
+    return;
+  }
+
+  // --------------------------------------------------------- compute warps
   const int k0 = (int)base + tid * ITEMS;
   const int cnt = max(0, min(ITEMS, a.n - k0));
-  // segment heads of this thread's row, from the descriptor's head bitmap
   unsigned heads = 0;
   if (cnt > 0) {
     if (SEG) {
@@ -377,8 +401,8 @@ __global__ void __launch_bounds__(TT, 768 / TT) k_scan_tma(const __grid_constant
     W = sl - sf + 2;
     if (W <= WMAX)
       for (int i = tid; i < W; i += TT) win[i] = __ldg(a.sv.off + sf + i);
+    named_sync(2, TT);  // window loaded
   }
-  __syncthreads();  // barrier initialised; window loaded
   {
     int it = 0;
     while (!mbar_try_wait(&bar, 0)) {
@@ -436,10 +460,11 @@ __global__ void __launch_bounds__(TT, 768 / TT) k_scan_tma(const __grid_constant
   T ev = shfl_up(v, 1);
   if (lane == 0) { ef = 0; ev = Op::ident(); }
   if (lane == 31) { s_wf[warp] = f; s_wv[warp] = v; }
-  __syncthreads();
+  named_sync(2, TT);
 
   if (warp == 0) {
-    // exclusive prefixes over the warps and the tile aggregate
+    // exclusive prefixes over the warps, the tile aggregate, and its
+    // publication for later tiles
     int wf = lane < NW ? s_wf[lane] : 0;
     T wv = lane < NW ? s_wv[lane] : Op::ident();
 #pragma unroll
@@ -454,16 +479,13 @@ __global__ void __launch_bounds__(TT, 768 / TT) k_scan_tma(const __grid_constant
     if (lane < NW) { s_wpf[lane] = xf; s_wpv[lane] = xv; }
     const int af = shfl_idx(wf, NW - 1);
     const T av = shfl_idx(wv, NW - 1);
-    const bool first_head = shfl_idx((int)(heads & 1u), 0) != 0;
-    if (lane == 0) lb_publish(a.lb.word + tile, (tile == 0 || af) ? TS_INC : TS_AGG, to_bits<T>(av));
-    T P = Op::ident();
-    if (tile > 0 && !first_head) {
-      P = lookback_prefix<Op>(a.lb.word, tile, a.status, a.spin_limit);
-      if (lane == 0 && !af) lb_publish(a.lb.word + tile, TS_INC, to_bits<T>(Op::apply(P, av)));
+    if (lane == 0) {
+      lb_publish(a.lb.word + tile, (tile == 0 || af) ? TS_INC : TS_AGG, to_bits<T>(av));
+      s_af = af;
+      s_av = av;
     }
-    if (lane == 0) s_prefix = P;
   }
-  __syncthreads();
+  named_sync(1, TB_LB);  // meet the look-back warp: carry and aggregate exchanged
   // this thread's exclusive prefix: (earlier tiles) . (earlier warps) . (earlier lanes)
   int pf = s_wpf[warp];
   T pv = s_wpv[warp];
@@ -492,7 +514,7 @@ __global__ void __launch_bounds__(TT, 768 / TT) k_scan_tma(const __grid_constant
         if (i < cnt) a.out[k0 + i] = x[i];
     }
     fence_proxy_async_smem();
-    __syncthreads();
+    named_sync(2, TT);
     if (tid == 0) {
       tma_store_2d(&tout, tile_b, 0, tile * TT);
       bulk_commit();
@@ -600,7 +622,7 @@ bool run_scan_tma(typename Op::T *out, const typename Op::T *in, vec_p sd, int n
   a.status = S.d_status;
   a.spin_limit = S.spin_limit;
   GCVL_CK(cudaMemsetAsync(mem, 0, lookback_clear_bytes(tiles), S.stream));
-  k_scan_tma<Op, MODE, SEG><<<tiles, TT, tma_smem<T>(), S.stream>>>(tin, tout, a);
+  k_scan_tma<Op, MODE, SEG><<<tiles, TB_LB, tma_smem<T>(), S.stream>>>(tin, tout, a);
   launch_check(name);
   return true;
 }
@@ -972,8 +994,8 @@ GCVL_EXPORT int gcvl_add_sed_noalloc(vec_p d, vec_p s, vec_p sd, int n, int m) {
     a.lb = lookback_carve(mem, tiles);
     a.status = g_noalloc_status_ptr[dev];
     a.spin_limit = S.spin_limit;
-    if (seg) k_scan_tma<AddD, M_SCAN, true><<<tiles, TT, tma_smem<double>(), strm>>>(tin, tout, a);
-    else k_scan_tma<AddD, M_SCAN, false><<<tiles, TT, tma_smem<double>(), strm>>>(tin, tout, a);
+    if (seg) k_scan_tma<AddD, M_SCAN, true><<<tiles, TB_LB, tma_smem<double>(), strm>>>(tin, tout, a);
+    else k_scan_tma<AddD, M_SCAN, false><<<tiles, TB_LB, tma_smem<double>(), strm>>>(tin, tout, a);
   } else {
     ScanArgs<double> a;
     a.out = out; a.in = in; a.out2 = nullptr; a.n = n;
@@ -990,3 +1012,11 @@ GCVL_EXPORT int gcvl_add_sed_noalloc(vec_p d, vec_p s, vec_p sd, int n, int m) {
 }
 
 GCVL_EXPORT long gcvl_add_sed_noalloc_max_n(void) { return kNoallocMaxN; }
+
+// add_ruz with the result left in device memory (d[0]), so that a sequence
+// needing a length (PACK, MAKE_SEGDES) can be captured in a CUDA graph: the
+// host reads the value once, after the graph, instead of synchronising inside.
+GCVL_EXPORT void gcvl_add_ruz_dev(vec_p d, vec_p s, int len, vec_p scratch) {
+  run_reduce<AddZ>((const int *)s, len, (int *)d, scratch, false);
+}
+GCVL_EXPORT int gcvl_add_ruz_dev_scratch(int len) { return reduce_units<int>(len); }
