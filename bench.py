@@ -241,6 +241,32 @@ def primitive_suite(g, n, hbm):
     return out
 
 
+def batched_suite(g, nvec=8192, total=1 << 27, seed=3):
+    """The batched workload: nvec segmented vectors of log-normal lengths in
+    [10, 10^6] (about `total` elements), half int32 and half float64, each
+    running +_scan, PACK by x > 0 and a random in-segment gather; per-vector
+    call loop against the flattened sequence and its CUDA-graph replay.
+    Wall-clock times of whole synchronised runs (the per-call loop reads a
+    count back to the host per vector)."""
+    from neslgpu_gb300 import batch as B
+    res = {"vectors": nvec, "elements": 0, "percall_ms": 0.0, "batched_ms": 0.0, "graph_ms": 0.0}
+    for half, dbl in ((0, False), (1, True)):
+        b = B.make_batch(nvec // 2, total // 2, seed=seed + half)
+        run = B.BatchRun(b, dbl, cvl=g.c)
+        try:
+            for mode in ("percall", "batched", "graph"):
+                res[f"{mode}_ms"] += run.timeit(mode, reps=3 if mode == "percall" else 10) * 1e3
+            res["elements"] += b.n
+        finally:
+            run.free()
+    for k in ("percall_ms", "batched_ms", "graph_ms"):
+        res[k] = round(res[k], 3)
+    res["graph_gelem_s"] = round(res["elements"] / (res["graph_ms"] * 1e-3) / 1e9, 2)
+    res["speedup_batched_vs_percall"] = round(res["percall_ms"] / res["batched_ms"], 2)
+    res["speedup_graph_vs_percall"] = round(res["percall_ms"] / res["graph_ms"], 2)
+    return res
+
+
 def cpu_baseline_port(x, lens, threads=1):
     """The oracle restatement of the serial CVL on this host: add_sed and
     add_red over the same values and segments.  With threads > 1 the
@@ -401,9 +427,10 @@ def gpu_arm(a):
         cpu["max_rel_diff_scan"] = float(np.max(np.abs(gs - scan) / np.maximum(np.abs(scan), 1.0)))
         cpu["max_rel_diff_reduce"] = float(np.max(np.abs(gr - red) / np.maximum(np.abs(red), 1.0)))
 
-    prims = None
+    prims = batched = None
     if not a.no_suite and rank == 0:
         prims = primitive_suite(g, n, hbm)
+        batched = batched_suite(g)
 
     if rank == 0:
         line = {
@@ -417,7 +444,7 @@ def gpu_arm(a):
                        "l2": "inputs larger than L2 (2 GiB per vector), no flush",
                        "parallelism": f"{world} independent replicas"},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
-            "clocks": clk.summary(w0, w1), "primitives": prims,
+            "clocks": clk.summary(w0, w1), "primitives": prims, "batched": batched,
         }
         print(json.dumps(line))
 
@@ -471,6 +498,7 @@ def main():
     ap.add_argument("--no-suite", action="store_true")
     ap.add_argument("--suite-only", action="store_true",
                     help="only the per-primitive table at 2^log2n (for profiling)")
+    ap.add_argument("--batched-only", action="store_true", help="only the batched workload")
     a = ap.parse_args()
     a.warmup = max(a.warmup, 3) if a.impl == "gb300" else a.warmup
     if a.impl == "reference":
@@ -479,6 +507,8 @@ def main():
     elif a.suite_only:
         g = Gpu()
         print(json.dumps({"primitives": primitive_suite(g, 1 << a.log2n, peaks()[0])}))
+    elif a.batched_only:
+        print(json.dumps({"batched": batched_suite(Gpu())}))
     else:
         gpu_arm(a)
 

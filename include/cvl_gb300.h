@@ -747,8 +747,9 @@ void gcvl_fill_random(vec_p d, long n, int kind, unsigned long long seed, double
 /* CUDA graphs over library calls: calls issued between gcvl_graph_begin and
  * gcvl_graph_end are captured from the library stream into one executable
  * graph (returned) instead of running.  Captured calls must not synchronise
- * (no *_ru*, ext_vu*, pk1_luv, c2v_fu*, v2c_fu*) and must be given scratch.
- * gcvl_graph_launch replays it on the library stream. */
+ * (no *_ru*, ext_vu*, rep_vu*, pk1_luv, c2v_fu*, v2c_fu*) and must be given
+ * scratch.  gcvl_graph_launch replays it on the library stream.  A captured
+ * rnd_wuz draws from the generator state at capture time on every replay. */
 int gcvl_graph_begin(void);
 void *gcvl_graph_end(void);
 int gcvl_graph_launch(void *graph);

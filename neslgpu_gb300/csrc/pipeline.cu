@@ -38,7 +38,7 @@ GCVL_EXPORT void gcvl_graph_destroy(void *exec) {
 // For each of nvec vectors (concatenated in x, inner segment lengths in
 // seg_lens, vector v owning nseg_of[v] segments), the sequence a VCODE
 // basic block issues through the CVL ABI:
-//   MAKE_SEGDES, +_SCAN, DIST 0, >, PACK (pk1_lev, +_REDUCE -> host,
+//   MAKE_SEGDES, +_SCAN of x, DIST 0, x > 0, PACK of the scan by those flags (pk1_lev, +_REDUCE -> host,
 //   MAKE_SEGDES, pk2_le), DIST of the new lengths, RAND, BPERMUTE
 // all on device vectors, one vector at a time.  Results land at the same
 // places as the batched form's, so the two can be compared.
@@ -77,7 +77,7 @@ static int percall(T *x, const int *seg_lens_host, const int *nseg_of, const int
     mke_fov(sd, lens_dev, n, m, work);
     pc_scan(y + eoff, x + eoff, sd, n, m, work);
     pc_dis((T *)zeros, n);
-    pc_grt(f + eoff, y + eoff, (T *)zeros, n);
+    pc_grt(f + eoff, x + eoff, (T *)zeros, n);
     pk1_lev(newlens + soff, f + eoff, sd, n, m, work);
     const int n2 = add_ruz(newlens + soff, m, work);  // host synchronisation, as in vinterp
     mke_fov(sd2, newlens + soff, n2, m, work);

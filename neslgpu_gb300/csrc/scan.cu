@@ -335,7 +335,7 @@ __device__ __forceinline__ double fx_range(const double (&x)[ITEMS], int from, i
 // exists and meet the look-back warp only when they need the carry.
 constexpr int TB_LB = TT + 32;  // threads per CTA
 template <class Op, int MODE, bool SEG>
-__global__ void __launch_bounds__(TB_LB, 5) k_scan_tma(const __grid_constant__ CUtensorMap tin,
+__global__ void __launch_bounds__(TB_LB, MODE == M_REDUCE ? 7 : 5) k_scan_tma(const __grid_constant__ CUtensorMap tin,
                                                      const __grid_constant__ CUtensorMap tout,
                                                      TArgs<typename Op::T> a) {
   typedef typename Op::T T;
