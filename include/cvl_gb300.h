@@ -782,6 +782,45 @@ int gcvl_pipeline_percall(int is_double, vec_p x, const int *seg_lens_host, cons
  * GCVL error code. */
 int gcvl_add_sed_noalloc(vec_p d, vec_p s, vec_p sd, int n, int m);
 long gcvl_add_sed_noalloc_max_n(void);
+/* Kernel variants of the segmented scans, reductions and ranks (no
+ * counterpart in the reference; they stand in for the entry points named by
+ * `prim`: add_sez, add_sed, max_sez, max_sed, add_rez, add_red, max_rez,
+ * max_red, rku_lez, rku_led, rkd_lez, rkd_led, with those functions'
+ * arguments).  Variant 0 is the default tile kernel; 1 and 2 give each
+ * segment to one CTA (2048- and 512-element chunks), 3 and 4 to one warp
+ * (256- and 64-element chunks); 5 ranks each segment in one CTA's shared
+ * memory and needs every segment to hold at most 2048 elements.  Integer,
+ * min/max and rank results are identical for every variant; float64 sums
+ * agree within the library's float64 tolerance.  gcvl_run_variant returns 0
+ * or a GCVL error code (5: unknown primitive or variant). */
+int gcvl_variant_count(void);
+int gcvl_variant_valid(const char *prim, int variant, int max_segment_length);
+int gcvl_variant_scratch(const char *prim, int n, int m);
+int gcvl_run_variant(const char *prim, int variant, vec_p d, vec_p s, vec_p sd, int n, int m,
+                     vec_p scratch);
+/* The learned dispatcher (no counterpart in the reference).  A features row
+ * is 16 floats describing a call (sizes, length statistics, a length
+ * histogram, the kind of primitive and element type) followed by 8 floats,
+ * 1 for each variant valid for it.  The model is an FP32 MLP (16 -> 64 ->
+ * 64 -> 8, ReLU, softmax over the valid variants) of gcvl_mlp_param_count()
+ * floats, trained by gcvl_mlp_train (Adam, soft targets T of N x 8 floats;
+ * params, moments -- 2P floats, zero at first -- and X, T, loss on the
+ * device) and evaluated by gcvl_mlp_infer (one class per row into cls_dev).
+ * gcvl_dispatch_set_model installs a model (P floats of host memory, NULL to
+ * remove it); gcvl_auto_run then runs the variant it picks for prim
+ * (gcvl_dispatch_choice: synchronises once per new (prim, descriptor
+ * address, n, m), then uses a cache).  Without a model the default kernel
+ * runs.  Return 0 or a GCVL error code. */
+int gcvl_mlp_param_count(void);
+int gcvl_mlp_feature_stride(void);
+int gcvl_mlp_classes(void);
+int gcvl_seg_features(const char *prim, vec_p sd, int n, int m, float *out_dev);
+int gcvl_mlp_train(float *params, float *moments, const float *X, const float *T, int N, int epochs, int batch,
+                   float lr, unsigned seed, int step0, float *loss_dev);
+int gcvl_mlp_infer(const float *params, const float *X, int N, int *cls_dev);
+int gcvl_dispatch_set_model(const float *params_host);
+int gcvl_dispatch_choice(const char *prim, vec_p sd, int n, int m);
+int gcvl_auto_run(const char *prim, vec_p d, vec_p s, vec_p sd, int n, int m, vec_p scratch);
 /* The 48-bit lrand48 state behind rnd_wuz. */
 unsigned long long gcvl_rand_state(void);
 void gcvl_set_rand_state(unsigned long long state);

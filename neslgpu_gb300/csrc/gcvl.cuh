@@ -62,7 +62,7 @@ enum ErrorCode {
   GCVL_ERR_RANGE = 5,
 };
 // bits of the device status word
-enum : unsigned { DEV_TIMEOUT = 1u };
+enum : unsigned { DEV_TIMEOUT = 1u, DEV_RANGE = 2u };  // DEV_RANGE: a kernel skipped input it cannot take
 
 inline int ceil_div(long a, long b) { return (int)((a + b - 1) / b); }
 inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
@@ -150,6 +150,20 @@ struct CountB { typedef int T;
 
 // ------------------------------------------------------- device helpers ---
 template <class T> __device__ __forceinline__ T shfl_up(T v, int d) { return __shfl_up_sync(0xffffffffu, v, d); }
+// Lanes of the warp holding the same 8-bit digit as this lane (digit < 0:
+// an empty lane, matched by nobody and matching nothing).  Eight ballots
+// instead of match.any, whose cost grows with the number of distinct values
+// and which runs on a narrow pipe: with 8-bit radix digits almost every lane
+// holds a different value.
+__device__ __forceinline__ unsigned warp_match8(int digit) {
+  unsigned peers = __ballot_sync(0xffffffffu, digit >= 0);
+#pragma unroll
+  for (int b = 0; b < 8; b++) {
+    const unsigned bal = __ballot_sync(0xffffffffu, (digit >> b) & 1);
+    peers &= ((digit >> b) & 1) ? bal : ~bal;
+  }
+  return digit >= 0 ? peers : 0u;
+}
 template <class T> __device__ __forceinline__ T shfl_down(T v, int d) { return __shfl_down_sync(0xffffffffu, v, d); }
 template <class T> __device__ __forceinline__ T shfl_idx(T v, int l) { return __shfl_sync(0xffffffffu, v, l); }
 
@@ -197,6 +211,9 @@ template <class T> __device__ __forceinline__ T ld_relaxed(const T *p) {
 //                             multiple of 256 words
 // with L0 = align4(m), L1 = L0 + align4(m + 1), L2 = L1 + align4(ng + 1),
 // ng = ceil(n / kGranule), nb = align256(ceil(n / 32)).
+// what a segmented pass produces: scan outputs, one result per segment, or
+// segment offsets (the scan of the lengths, in mke_fov)
+enum Mode { M_SCAN = 0, M_REDUCE = 1, M_OFFSETS = 2 };
 constexpr int kGranule = 64;
 struct SegView {
   const int *len;
@@ -264,6 +281,14 @@ inline LookbackMem lookback_carve(void *base, int tiles) {
 }
 // scratch units (8 bytes) needed by a look-back launch of `tiles` tiles
 inline int lookback_units(int tiles) { return (int)((lookback_bytes(tiles) + 7) / 8); }
+
+// Partitioned scatter (rank.cu): d[idx[k]] = s[k] for k < n, idx in
+// [0, n_d), by a partition of (index, value) pairs into 256 windows of the
+// output and a window-by-window scatter.  Worth it once the output is larger
+// than L2 can absorb random writes to; scratch of scatter_partitioned_bytes.
+bool scatter_partitioned_wanted(long n_d, size_t vsize);
+size_t scatter_partitioned_bytes(long n, size_t vsize);
+template <class V> void scatter_partitioned(V *d, const V *s, const int *idx, int n, int n_d, vec_p scratch);
 
 __device__ __forceinline__ void lb_publish(ulonglong2 *w, unsigned long long status, unsigned long long bits) {
   asm volatile("{\n .reg .b128 t;\n mov.b128 t, {%1, %2};\n st.relaxed.gpu.global.b128 [%0], t;\n}"

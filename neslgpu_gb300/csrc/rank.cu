@@ -1,5 +1,6 @@
 // rank.cu -- stable radix rank, up and down, int and double, segmented and
-// unsegmented (nesl/cvl/serial/rank.c:49-362).
+// unsegmented (nesl/cvl/serial/rank.c:49-362), and the partitioned scatter
+// that large permutes share with it.
 //
 // d[j] is the position of element j in the stable sorted order of its
 // segment.  Keys are made order-preserving unsigned integers exactly as the
@@ -9,13 +10,24 @@
 // segmented rank is a stable sort by (segment, key): the key passes carry
 // each element's segment number, then further passes sort by it.
 //
-// GPU design (onesweep style): one prepare pass writes transformed keys and
-// indices and builds every pass's 256-bin digit histogram at once with
-// shared-memory atomics.  Then one scatter pass per 8-bit digit: each CTA
-// ranks its tile stably with warp match/ballot, learns how many earlier
-// tiles' elements fall in each digit by a per-digit decoupled look-back,
-// reorders the tile in shared memory and writes coalesced runs.  The last
-// pass writes d[index] = position directly.
+// GPU design (onesweep style).  One prepare pass builds every pass's 256-bin
+// digit histogram at once with shared-memory atomics (and, for segmented
+// ranks, writes transformed keys, indices and segment numbers).  Then one
+// pass per 8-bit digit: a CTA stages its 4096-element tile in shared memory,
+// ranks it stably per warp with ballots, learns how many earlier tiles'
+// elements fall in each digit by a per-digit decoupled look-back, reorders
+// the tile in shared memory and writes coalesced runs.  The first pass of an
+// unsegmented rank reads the caller's keys and transforms them itself.
+//
+// The result is the inverse of the sort permutation: rank[index] = position,
+// a scatter to random places.  Below RK_DIRECT_MAX elements the last pass
+// writes it directly (the rank vector fits in L2, which absorbs the random
+// writes).  Above it the last pass writes (index, position) pairs in sorted
+// order, one more pass partitions them by the top 8 bits of the index --
+// 256 windows of the output -- and a streaming kernel writes each window's
+// ranks while the window sits in L2, so DRAM sees whole sectors instead of a
+// read-modify-write per 4-byte element.  smp_pu* uses the same partition and
+// window scatter for large vectors.
 #include "gcvl.cuh"
 
 #include <utility>
@@ -25,12 +37,24 @@ namespace gcvl {
 constexpr int RK_BLOCK = 256, RK_ITEMS = 16, RK_TILE = RK_BLOCK * RK_ITEMS;
 constexpr int RK_WARPS = RK_BLOCK / 32;
 constexpr int RK_MAXPASS = 12;
-constexpr int RK_LB = 8;  // predecessors read per look-back round trip
-enum : unsigned long long { RK_AGG = 1ULL << 62, RK_INC = 2ULL << 62, RK_MASK = (1ULL << 62) - 1 };
+constexpr int RK_LB = 32;  // predecessors read per look-back round trip
+constexpr int RK_DIRECT_MAX = 1 << 23;
+constexpr int SC_ITEMS = 8;  // elements per thread in the streaming scatter
+constexpr unsigned RK_INC = 0x80000000u;
+
+// where a pass gets its tile from, and where it puts it
+enum { IN_ARRAYS = 0, IN_SRC = 1 };                    // IN_SRC: caller's keys, value = position
+enum { OUT_ARRAYS = 0, OUT_RANK = 1, OUT_PAIRS = 2 };  // OUT_RANK: rank[v] = pos; OUT_PAIRS: (v, pos)
+
+__host__ __device__ inline int bit_length(unsigned x) {
+  int b = 0;
+  while (x) { b++; x >>= 1; }
+  return b;
+}
 
 struct RankPrep {
   const void *src;
-  int n, is_double, up, seg;
+  int n, is_double, up, seg, write_arrays;
   SegView sv;
   void *key;           // uint32 or uint64 transformed keys
   unsigned *idx;
@@ -43,6 +67,30 @@ __device__ __forceinline__ unsigned long long rk_key64(unsigned long long b, int
   unsigned long long k = (b >> 63) ? ~b : (b ^ (1ULL << 63));
   return up ? k : ~k;
 }
+__device__ __forceinline__ unsigned rk_key32(unsigned x, int up) { return x ^ (up ? 0x80000000u : 0x7FFFFFFFu); }
+
+__device__ __forceinline__ void rank_prep_one(const RankPrep &p, unsigned *s_hist, long i, unsigned long long raw) {
+  unsigned long long k;
+  if (p.is_double) {
+    k = rk_key64(raw, p.up);
+    if (p.write_arrays) ((unsigned long long *)p.key)[i] = k;
+  } else {
+    const unsigned kk = rk_key32((unsigned)raw, p.up);
+    if (p.write_arrays) ((unsigned *)p.key)[i] = kk;
+    k = kk;
+  }
+  if (p.write_arrays) p.idx[i] = (unsigned)i;
+  for (int q = 0; q < p.key_passes; q++) atomicAdd(&s_hist[q * 256 + (int)((k >> (8 * q)) & 255)], 1u);
+  if (p.seg) {
+    const unsigned sg = (unsigned)seg_of(p.sv, (int)i);
+    p.aux[i] = sg;
+    for (int q = 0; q < p.seg_passes; q++)
+      atomicAdd(&s_hist[(p.key_passes + q) * 256 + ((sg >> (8 * q)) & 255)], 1u);
+  }
+}
+__device__ __forceinline__ unsigned long long rank_prep_load(const RankPrep &p, long i) {
+  return p.is_double ? __ldcs((const unsigned long long *)p.src + i) : (unsigned long long)__ldcs((const unsigned *)p.src + i);
+}
 
 __global__ void __launch_bounds__(RK_BLOCK) k_rank_prep(RankPrep p) {
   __shared__ unsigned s_hist[RK_MAXPASS * 256];
@@ -50,29 +98,31 @@ __global__ void __launch_bounds__(RK_BLOCK) k_rank_prep(RankPrep p) {
   for (int i = threadIdx.x; i < passes * 256; i += RK_BLOCK) s_hist[i] = 0;
   __syncthreads();
   const long stride = (long)gridDim.x * RK_BLOCK;
-  for (long i = (long)blockIdx.x * RK_BLOCK + threadIdx.x; i < p.n; i += stride) {
-    unsigned long long k;
-    if (p.is_double) {
-      k = rk_key64(((const unsigned long long *)p.src)[i], p.up);
-      ((unsigned long long *)p.key)[i] = k;
-    } else {
-      unsigned x = ((const unsigned *)p.src)[i];
-      unsigned kk = x ^ (p.up ? 0x80000000u : 0x7FFFFFFFu);
-      ((unsigned *)p.key)[i] = kk;
-      k = kk;
-    }
-    p.idx[i] = (unsigned)i;
-    for (int q = 0; q < p.key_passes; q++) atomicAdd(&s_hist[q * 256 + (int)((k >> (8 * q)) & 255)], 1u);
-    if (p.seg) {
-      unsigned sg = (unsigned)seg_of(p.sv, (int)i);
-      p.aux[i] = sg;
-      for (int q = 0; q < p.seg_passes; q++)
-        atomicAdd(&s_hist[(p.key_passes + q) * 256 + ((sg >> (8 * q)) & 255)], 1u);
-    }
+  long i = (long)blockIdx.x * RK_BLOCK + threadIdx.x;
+  // four independent loads in flight per thread
+  for (; i + 3 * stride < p.n; i += 4 * stride) {
+    unsigned long long r[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) r[u] = rank_prep_load(p, i + u * stride);
+#pragma unroll
+    for (int u = 0; u < 4; u++) rank_prep_one(p, s_hist, i + u * stride, r[u]);
   }
+  for (; i < p.n; i += stride) rank_prep_one(p, s_hist, i, rank_prep_load(p, i));
   __syncthreads();
   for (int i = threadIdx.x; i < passes * 256; i += RK_BLOCK)
     if (s_hist[i]) atomicAdd(&p.hist[i], s_hist[i]);
+}
+
+// histogram of one digit of 32-bit keys (the partition of a scatter)
+__global__ void __launch_bounds__(RK_BLOCK) k_digit_hist(const unsigned *key, long n, int shift, unsigned *hist) {
+  __shared__ unsigned s_hist[256];
+  s_hist[threadIdx.x] = 0;
+  __syncthreads();
+  const long stride = (long)gridDim.x * RK_BLOCK;
+  for (long i = (long)blockIdx.x * RK_BLOCK + threadIdx.x; i < n; i += stride)
+    atomicAdd(&s_hist[(__ldcs(key + i) >> shift) & 255], 1u);
+  __syncthreads();
+  if (s_hist[threadIdx.x]) atomicAdd(&hist[threadIdx.x], s_hist[threadIdx.x]);
 }
 
 // hist[q][d] -> exclusive scan over d, in place (one CTA, 256 threads)
@@ -93,29 +143,47 @@ __global__ void k_rank_digit_starts(unsigned *hist, int passes) {
   }
 }
 
-template <class K> struct PassArgs {
-  const K *kin; const unsigned *iin; const unsigned *ain;
-  K *kout; unsigned *iout; unsigned *aout;
-  int *rank;           // final pass output
-  const int *segoff;   // final pass of a segmented rank: segment offsets
-  const unsigned *starts;  // this pass's digit starts
-  unsigned long long *state;  // [tiles][256]
+// digit starts of a permutation of [0, n) split by index >> shift: every
+// window but the last is full
+__global__ void k_window_starts(unsigned *starts, int n, int shift) {
+  const long s = (long)threadIdx.x << shift;
+  starts[threadIdx.x] = (unsigned)(s < n ? s : n);
+}
+
+template <class K, class V> struct PassArgs {
+  const K *kin; const V *vin; const unsigned *ain;
+  K *kout; V *vout; unsigned *aout;
+  const void *src; int up;            // IN_SRC: the caller's keys
+  int *rank; const int *segoff;       // OUT_RANK / OUT_PAIRS (segmented: rebase by the key)
+  unsigned *pidx, *ppos;              // OUT_PAIRS
+  const unsigned *starts;             // this pass's digit starts
+  unsigned *state;                    // [tiles][256] look-back words
   unsigned *counter;
   int n, shift;
   unsigned *status;
   int spin_limit;
 };
 
-template <class K, bool AUX, bool FINAL>
-__global__ void __launch_bounds__(RK_BLOCK) k_rank_pass(PassArgs<K> a) {
+template <class K, class V, bool AUX> constexpr size_t pass_smem() {
+  return (size_t)RK_TILE * (2 * sizeof(K) + 2 * sizeof(V) + (AUX ? 8 : 0)) + RK_WARPS * 256 * 2 + 256 * 4 +
+         256 * 8;
+}
+
+template <class K, class V, bool AUX, int IN, int OUT>
+__global__ void __launch_bounds__(RK_BLOCK, 2) k_radix_pass(PassArgs<K, V> a) {
   extern __shared__ __align__(16) unsigned char rk_smem[];
-  K *s_key = (K *)rk_smem;
-  unsigned *s_idx = (unsigned *)(s_key + RK_TILE);
-  unsigned *s_aux = s_idx + RK_TILE;
-  unsigned *s_cnt = s_aux + (AUX ? RK_TILE : 0);  // [RK_WARPS][256]
-  unsigned *s_loc = s_cnt + RK_WARPS * 256;        // local digit offsets
-  long long *s_gb = (long long *)(s_loc + 256);    // global base per digit
+  // staged tile (input order) and the reordered tile
+  long long *s_gb = (long long *)rk_smem;                  // [256] global base per digit
+  K *s_kin = (K *)(s_gb + 256);
+  K *s_kout = s_kin + RK_TILE;
+  V *s_vin = (V *)(s_kout + RK_TILE);
+  V *s_vout = s_vin + RK_TILE;
+  unsigned *s_ain = (unsigned *)(s_vout + RK_TILE);
+  unsigned *s_aout = s_ain + (AUX ? RK_TILE : 0);
+  unsigned *s_loc = s_aout + (AUX ? RK_TILE : 0);          // [256] tile offset per digit
+  unsigned short *s_cnt = (unsigned short *)(s_loc + 256);  // [RK_WARPS][256]
   __shared__ unsigned s_tile;
+  __shared__ unsigned s_ws[RK_WARPS];
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   if (tid == 0) s_tile = atomicAdd(a.counter, 1u);
@@ -125,35 +193,42 @@ __global__ void __launch_bounds__(RK_BLOCK) k_rank_pass(PassArgs<K> a) {
   const long base = (long)tile * RK_TILE;
   const int valid = (int)min((long)RK_TILE, (long)a.n - base);
 
-  // this warp's contiguous range, 32 elements per step
-  K key[RK_ITEMS];
-  unsigned idx[RK_ITEMS], aux[RK_ITEMS], wr[RK_ITEMS];
-  int dig[RK_ITEMS];
-  const int wbase = warp * 32 * RK_ITEMS;
+  // stage the tile: every load of the thread in flight at once
 #pragma unroll
   for (int c = 0; c < RK_ITEMS; c++) {
-    int e = wbase + c * 32 + lane;
+    const int e = c * RK_BLOCK + tid;
     if (e < valid) {
-      key[c] = __ldcs(a.kin + base + e);
-      idx[c] = __ldcs(a.iin + base + e);
-      if (AUX) aux[c] = __ldcs(a.ain + base + e);
-      dig[c] = (int)((key[c] >> a.shift) & 255);
-    } else {
-      dig[c] = -1;
+      if constexpr (IN == IN_SRC) {
+        if constexpr (sizeof(K) == 8)
+          s_kin[e] = (K)rk_key64(__ldcs((const unsigned long long *)a.src + base + e), a.up);
+        else
+          s_kin[e] = (K)rk_key32(__ldcs((const unsigned *)a.src + base + e), a.up);
+        s_vin[e] = (V)(base + e);
+      } else {
+        s_kin[e] = __ldcs(a.kin + base + e);
+        s_vin[e] = __ldcs(a.vin + base + e);
+        if (AUX) s_ain[e] = __ldcs(a.ain + base + e);
+      }
     }
   }
-  unsigned *cnt = s_cnt + warp * 256;
+  __syncthreads();
+
+  // stable rank within each warp's 512 elements: (rank << 8) | digit
+  const int wbase = warp * 32 * RK_ITEMS;
+  unsigned short *cnt = s_cnt + warp * 256;
   const unsigned lt = (1u << lane) - 1u;
+  unsigned wr[RK_ITEMS];
 #pragma unroll
   for (int c = 0; c < RK_ITEMS; c++) {
-    int d = dig[c];
-    unsigned peers = __match_any_sync(0xffffffffu, d);
+    const int e = wbase + c * 32 + lane;
+    const int d = e < valid ? (int)((s_kin[e] >> a.shift) & 255) : -1;
+    const unsigned peers = warp_match8(d);
     unsigned r = 0;
     if (d >= 0) r = cnt[d] + __popc(peers & lt);
     __syncwarp();
-    if (d >= 0 && (peers & lt) == 0) cnt[d] += __popc(peers);
+    if (d >= 0 && (peers & lt) == 0) cnt[d] = (unsigned short)(cnt[d] + __popc(peers));
     __syncwarp();
-    wr[c] = r;
+    wr[c] = d >= 0 ? (r << 8) | (unsigned)d : 0xFFFFFFFFu;
   }
   __syncthreads();
 
@@ -163,31 +238,34 @@ __global__ void __launch_bounds__(RK_BLOCK) k_rank_pass(PassArgs<K> a) {
 #pragma unroll
   for (int w = 0; w < RK_WARPS; w++) {
     unsigned c = s_cnt[w * 256 + dd];
-    s_cnt[w * 256 + dd] = tot;
+    s_cnt[w * 256 + dd] = (unsigned short)tot;
     tot += c;
   }
-  // publish this tile's digit count, then look back for earlier tiles'
-  unsigned long long *st = a.state + (long)tile * 256 + dd;
+  // publish this tile's digit count, then look back for earlier tiles'.
+  // One 32-bit word per (tile, digit): 0 = not yet, 1 + count = this tile's
+  // count (aggregate), RK_INC | prefix = count of this digit in this and all
+  // earlier tiles (inclusive; < 2^31 because n is an int).
+  unsigned *stw = a.state + (long)tile * 256 + dd;
   if (tile == 0) {
-    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(st), "l"(RK_INC | tot) : "memory");
+    asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(stw), "r"(RK_INC | tot) : "memory");
   } else {
-    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(st), "l"(RK_AGG | tot) : "memory");
+    asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(stw), "r"(1u + tot) : "memory");
   }
   // look back for this digit: RK_LB predecessors per round trip, nearest
-  // first, until an inclusive count is found (bounded waits).  Each status
-  // word is self-contained, so relaxed loads suffice and all RK_LB are in
-  // flight together.
-  unsigned long long prefix = 0;
+  // first, until an inclusive count is found (bounded waits).  Each word is
+  // self-contained, so relaxed loads suffice and all RK_LB are in flight
+  // together; a warp's loads of one predecessor are one 128-byte line.
+  unsigned prefix = 0;
   if (tile > 0) {
     long t0 = tile - 1;
     bool done = false;
     while (!done && t0 >= 0) {
-      unsigned long long w[RK_LB];
+      unsigned w[RK_LB];
 #pragma unroll
       for (int j = 0; j < RK_LB; j++) {
         w[j] = RK_INC;  // beyond tile 0: an inclusive zero
         if (t0 - j >= 0)
-          asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(w[j]) : "l"(a.state + (t0 - j) * 256 + dd) : "memory");
+          asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(w[j]) : "l"(a.state + (t0 - j) * 256 + dd) : "memory");
       }
 #pragma unroll
       for (int j = 0; j < RK_LB; j++) {
@@ -196,30 +274,29 @@ __global__ void __launch_bounds__(RK_BLOCK) k_rank_pass(PassArgs<K> a) {
         while (w[j] == 0) {
           if (++it >= a.spin_limit) { atomicOr(a.status, DEV_TIMEOUT); w[j] = RK_INC; break; }
           __nanosleep(32);
-          asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(w[j]) : "l"(a.state + (t0 - j) * 256 + dd) : "memory");
+          asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(w[j]) : "l"(a.state + (t0 - j) * 256 + dd) : "memory");
         }
-        prefix += w[j] & RK_MASK;
-        if (w[j] & RK_INC) done = true;
+        if (w[j] & RK_INC) { prefix += w[j] & ~RK_INC; done = true; }
+        else prefix += w[j] - 1u;
       }
       t0 -= RK_LB;
     }
-    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(st), "l"(RK_INC | (prefix + tot)) : "memory");
+    asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(stw), "r"(RK_INC | (prefix + tot)) : "memory");
   }
-  // exclusive scan of tile counts over the digits -> local offsets
+  // exclusive scan of tile counts over the digits -> tile offsets
   {
-    unsigned v = tot, incl = v;
+    unsigned incl = tot;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
       unsigned x = shfl_up(incl, o);
       if (lane >= o) incl += x;
     }
-    __shared__ unsigned s_ws[RK_WARPS];
     if (lane == 31) s_ws[warp] = incl;
     __syncthreads();
     unsigned wp = 0;
 #pragma unroll
     for (int w = 0; w < RK_WARPS; w++) if (w < warp) wp += s_ws[w];
-    unsigned loc = wp + incl - v;
+    const unsigned loc = wp + incl - tot;
     s_loc[dd] = loc;
     s_gb[dd] = (long long)__ldg(a.starts + dd) + (long long)prefix - (long long)loc;
   }
@@ -227,49 +304,134 @@ __global__ void __launch_bounds__(RK_BLOCK) k_rank_pass(PassArgs<K> a) {
   // reorder the tile in shared memory
 #pragma unroll
   for (int c = 0; c < RK_ITEMS; c++) {
-    int d = dig[c];
-    if (d >= 0) {
-      unsigned lp = s_loc[d] + s_cnt[warp * 256 + d] + wr[c];
-      s_key[lp] = key[c];
-      s_idx[lp] = idx[c];
-      if (AUX) s_aux[lp] = aux[c];
+    const unsigned x = wr[c];
+    if (x != 0xFFFFFFFFu) {
+      const int d = (int)(x & 255u);
+      const unsigned lp = s_loc[d] + s_cnt[warp * 256 + d] + (x >> 8);
+      const int e = wbase + c * 32 + lane;
+      s_kout[lp] = s_kin[e];
+      s_vout[lp] = s_vin[e];
+      if (AUX) s_aout[lp] = s_ain[e];
     }
   }
   __syncthreads();
   // coalesced runs out
+#pragma unroll 4
   for (int e = tid; e < valid; e += RK_BLOCK) {
-    K k = s_key[e];
-    int d = (int)((k >> a.shift) & 255);
-    long g = s_gb[d] + e;
-    if (FINAL) {
+    const K k = s_kout[e];
+    const int d = (int)((k >> a.shift) & 255);
+    const long g = s_gb[d] + e;
+    if (OUT == OUT_ARRAYS) {
+      a.kout[g] = k;
+      a.vout[g] = s_vout[e];
+      if (AUX) a.aout[g] = s_aout[e];
+    } else {
       int r = (int)g;
       if (a.segoff) r -= __ldg(a.segoff + (int)k);
-      a.rank[s_idx[e]] = r;
-    } else {
-      a.kout[g] = k;
-      a.iout[g] = s_idx[e];
-      if (AUX) a.aout[g] = s_aux[e];
+      if (OUT == OUT_RANK) {
+        a.rank[(unsigned)s_vout[e]] = r;
+      } else {
+        a.pidx[g] = (unsigned)s_vout[e];
+        a.ppos[g] = (unsigned)r;
+      }
     }
   }
 }
 
-template <class K, bool AUX, bool FINAL> size_t pass_smem() {
-  return (size_t)RK_TILE * sizeof(K) + (size_t)RK_TILE * 4 * (AUX ? 2 : 1) + RK_WARPS * 256 * 4 +
-         256 * 4 + 256 * 8;
+// d[key[i]] = val[i], streaming over pairs that a partition pass grouped by
+// output window
+template <class V>
+__global__ void __launch_bounds__(RK_BLOCK) k_window_scatter(V *__restrict__ d, const unsigned *__restrict__ key,
+                                                             const V *__restrict__ val, long n) {
+  const long i0 = (long)blockIdx.x * (RK_BLOCK * SC_ITEMS) + threadIdx.x;
+  unsigned k[SC_ITEMS];
+  V v[SC_ITEMS];
+#pragma unroll
+  for (int u = 0; u < SC_ITEMS; u++) {
+    const long i = i0 + (long)u * RK_BLOCK;
+    if (i < n) { k[u] = __ldcs(key + i); v[u] = __ldcs(val + i); }
+  }
+#pragma unroll
+  for (int u = 0; u < SC_ITEMS; u++) {
+    const long i = i0 + (long)u * RK_BLOCK;
+    if (i < n) d[k[u]] = v[u];
+  }
 }
 
-template <class K, bool AUX, bool FINAL>
-void launch_pass(PassArgs<K> a, int tiles) {
-  size_t sm = pass_smem<K, AUX, FINAL>();
+template <class K, class V, bool AUX, int IN, int OUT>
+void launch_pass(const PassArgs<K, V> &a, int tiles) {
+  constexpr size_t sm = pass_smem<K, V, AUX>();
   static bool attr = false;
   if (!attr) {
-    GCVL_CK(cudaFuncSetAttribute(k_rank_pass<K, AUX, FINAL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    GCVL_CK(cudaFuncSetAttribute(k_radix_pass<K, V, AUX, IN, OUT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)sm));
     attr = true;
   }
-  k_rank_pass<K, AUX, FINAL><<<tiles, RK_BLOCK, sm, stream()>>>(a);
-  launch_check("k_rank_pass");
+  k_radix_pass<K, V, AUX, IN, OUT><<<tiles, RK_BLOCK, sm, stream()>>>(a);
+  launch_check("k_radix_pass");
 }
 
+inline int rk_tiles(long n) { return (int)((n + RK_TILE - 1) / RK_TILE); }
+inline size_t rk_state_bytes(long n) { return (size_t)rk_tiles(n) * 256 * 4; }
+// top-8-bit windows of [0, n)
+inline int window_shift(int n) { int b = bit_length((unsigned)(n > 1 ? n - 1 : 1)); return b > 8 ? b - 8 : 0; }
+
+// ------------------------------------------------ partitioned scatter ---
+// d[idx[k]] = s[k] for k < n (idx in [0, n_d)): partition (idx, value) by
+// the top 8 bits of the index, then scatter window by window.
+struct ScatterLayout { size_t kout, vout, hist, counter, state, total; };
+inline ScatterLayout scatter_layout(long n, size_t vsize) {
+  ScatterLayout L;
+  size_t o = 0;
+  auto take = [&](size_t bytes) { size_t at = o; o += align_up(bytes, 256); return at; };
+  L.kout = take((size_t)n * 4);
+  L.vout = take((size_t)n * vsize);
+  L.hist = take(256 * 4);
+  L.counter = take(256);
+  L.state = take(rk_state_bytes(n));
+  L.total = o + 256;  // room to align the base
+  return L;
+}
+bool scatter_partitioned_wanted(long n_d, size_t vsize) { return (size_t)n_d * vsize > (size_t)RK_DIRECT_MAX * 4; }
+size_t scatter_partitioned_bytes(long n, size_t vsize) { return scatter_layout(n, vsize).total; }
+
+template <class V>
+void scatter_partitioned(V *d, const V *s, const int *idx, int n, int n_d, vec_p scratch) {
+  State &S = st();
+  if (n <= 0) return;
+  ScatterLayout L = scatter_layout(n, sizeof(V));
+  char *raw = (char *)scratch_or_work(scratch, L.total);
+  if (!raw) return;
+  char *mem = (char *)align_up((size_t)raw, 256);
+  unsigned *hist = (unsigned *)(mem + L.hist);
+  unsigned *counter = (unsigned *)(mem + L.counter);
+  unsigned *state = (unsigned *)(mem + L.state);
+  const int shift = window_shift(n_d);
+  const int tiles = rk_tiles(n);
+  GCVL_CK(cudaMemsetAsync(hist, 0, 256 * 4, S.stream));
+  GCVL_CK(cudaMemsetAsync(counter, 0, 4, S.stream));
+  GCVL_CK(cudaMemsetAsync(state, 0, rk_state_bytes(n), S.stream));
+  int hg = S.sm_count * 4;
+  if ((long)hg * RK_BLOCK > n) hg = (n + RK_BLOCK - 1) / RK_BLOCK;
+  k_digit_hist<<<hg, RK_BLOCK, 0, S.stream>>>((const unsigned *)idx, n, shift, hist);
+  launch_check("k_digit_hist");
+  k_rank_digit_starts<<<1, 256, 0, S.stream>>>(hist, 1);
+  launch_check("k_rank_digit_starts");
+  PassArgs<unsigned, V> a{};
+  a.kin = (const unsigned *)idx; a.vin = s;
+  a.kout = (unsigned *)(mem + L.kout); a.vout = (V *)(mem + L.vout);
+  a.starts = hist; a.state = state; a.counter = counter;
+  a.n = n; a.shift = shift; a.status = S.d_status; a.spin_limit = S.spin_limit;
+  launch_pass<unsigned, V, false, IN_ARRAYS, OUT_ARRAYS>(a, tiles);
+  const long g = ((long)n + RK_BLOCK * SC_ITEMS - 1) / (RK_BLOCK * SC_ITEMS);
+  k_window_scatter<V><<<(int)g, RK_BLOCK, 0, S.stream>>>(d, a.kout, a.vout, n);
+  launch_check("k_window_scatter");
+}
+template void scatter_partitioned<unsigned>(unsigned *, const unsigned *, const int *, int, int, vec_p);
+template void scatter_partitioned<unsigned long long>(unsigned long long *, const unsigned long long *,
+                                                      const int *, int, int, vec_p);
+
+// ------------------------------------------------------------- rank ---
 struct RankLayout {
   size_t key_a, key_b, idx_a, idx_b, aux_a, aux_b, hist, state, counter, total;
 };
@@ -284,11 +446,10 @@ inline RankLayout rank_layout(int n, int is_double, int seg) {
   L.idx_b = take((size_t)n * 4);
   L.aux_a = take(seg ? (size_t)n * 4 : 0);
   L.aux_b = take(seg ? (size_t)n * 4 : 0);
-  L.hist = take(RK_MAXPASS * 256 * 4);
-  L.counter = take(RK_MAXPASS * 4);
-  int tiles = (n + RK_TILE - 1) / RK_TILE;
-  L.state = take((size_t)tiles * 256 * 8);
-  L.total = o;
+  L.hist = take((RK_MAXPASS + 1) * 256 * 4);  // every pass's digit starts, then the window starts
+  L.counter = take((RK_MAXPASS + 1) * 4);
+  L.state = take(rk_state_bytes(n));
+  L.total = o + 256;  // room to align the base
   return L;
 }
 int rank_units(int n, int is_double, int seg) {
@@ -303,30 +464,31 @@ void rank_impl(vec_p d, vec_p s, vec_p sd, int n, int m, vec_p scratch, int is_d
   if (n <= 0) return;
   const bool seg = sd != nullptr && m > 1;
   RankLayout L = rank_layout(n, is_double, seg);
-  char *mem = (char *)scratch_or_work(scratch, L.total);
-  if (!mem) return;
+  char *raw = (char *)scratch_or_work(scratch, L.total);
+  if (!raw) return;
+  char *mem = (char *)align_up((size_t)raw, 256);
   const int key_passes = is_double ? 8 : 4;
   int seg_passes = 0;
-  if (seg) {
-    unsigned mm = (unsigned)(m - 1);
-    int bits = mm ? 32 - __builtin_clz(mm) : 1;
-    seg_passes = (bits + 7) / 8;
-  }
+  if (seg) seg_passes = (bit_length((unsigned)(m - 1)) + 7) / 8;
+  if (seg && seg_passes == 0) seg_passes = 1;
   const int passes = key_passes + seg_passes;
-  const int tiles = (n + RK_TILE - 1) / RK_TILE;
+  const int tiles = rk_tiles(n);
+  const bool direct = n <= RK_DIRECT_MAX;
   unsigned *hist = (unsigned *)(mem + L.hist);
   unsigned *counters = (unsigned *)(mem + L.counter);
-  unsigned long long *state = (unsigned long long *)(mem + L.state);
+  unsigned *state = (unsigned *)(mem + L.state);
   GCVL_CK(cudaMemsetAsync(hist, 0, RK_MAXPASS * 256 * 4, S.stream));
-  GCVL_CK(cudaMemsetAsync(counters, 0, RK_MAXPASS * 4, S.stream));
+  GCVL_CK(cudaMemsetAsync(counters, 0, (RK_MAXPASS + 1) * 4, S.stream));
 
+  // histograms of every pass (and, segmented, the staged keys)
   RankPrep p;
   p.src = s; p.n = n; p.is_double = is_double; p.up = up; p.seg = seg ? 1 : 0;
+  p.write_arrays = seg ? 1 : 0;
   p.sv = seg ? seg_view(sd, n, m) : SegView{nullptr, nullptr, nullptr, nullptr, n, 1};
   p.key = mem + L.key_a; p.idx = (unsigned *)(mem + L.idx_a);
   p.aux = seg ? (unsigned *)(mem + L.aux_a) : nullptr;
   p.hist = hist; p.key_passes = key_passes; p.seg_passes = seg_passes;
-  int pg = S.sm_count * 4;
+  int pg = S.sm_count * 8;
   long need = ((long)n + RK_BLOCK - 1) / RK_BLOCK;
   if (pg > need) pg = (int)need;
   k_rank_prep<<<pg, RK_BLOCK, 0, S.stream>>>(p);
@@ -339,36 +501,68 @@ void rank_impl(vec_p d, vec_p s, vec_p sd, int n, int m, vec_p scratch, int is_d
   unsigned *iA = (unsigned *)(mem + L.idx_a), *iB = (unsigned *)(mem + L.idx_b);
   unsigned *aA = seg ? (unsigned *)(mem + L.aux_a) : nullptr, *aB = seg ? (unsigned *)(mem + L.aux_b) : nullptr;
   const int *segoff = seg ? seg_view(sd, n, m).off : nullptr;
+  // last pass output when the ranks go through the window partition: the
+  // pair arrays take the buffers the last pass does not read
+  unsigned *pidx = nullptr, *ppos = nullptr;
   for (int q = 0; q < passes; q++) {
-    GCVL_CK(cudaMemsetAsync(state, 0, (size_t)tiles * 256 * 8, S.stream));
+    GCVL_CK(cudaMemsetAsync(state, 0, rk_state_bytes(n), S.stream));
     const bool final = (q == passes - 1);
     const bool keypass = q < key_passes;
+    if (final) { pidx = iB; ppos = (unsigned *)kB; }
     if (keypass) {
-      PassArgs<K> a{};
-      a.kin = (const K *)kA; a.iin = iA; a.ain = aA;
-      a.kout = (K *)kB; a.iout = iB; a.aout = aB;
-      a.rank = (int *)d; a.segoff = nullptr;
+      PassArgs<K, unsigned> a{};
+      a.kin = (const K *)kA; a.vin = iA; a.ain = aA;
+      a.kout = (K *)kB; a.vout = iB; a.aout = aB;
+      a.src = s; a.up = up;
+      a.rank = (int *)d; a.segoff = nullptr; a.pidx = pidx; a.ppos = ppos;
       a.starts = hist + q * 256; a.state = state; a.counter = counters + q;
       a.n = n; a.shift = 8 * q; a.status = S.d_status; a.spin_limit = S.spin_limit;
-      if (final) launch_pass<K, false, true>(a, tiles);
-      else if (seg) launch_pass<K, true, false>(a, tiles);
-      else launch_pass<K, false, false>(a, tiles);
+      if (seg) {
+        launch_pass<K, unsigned, true, IN_ARRAYS, OUT_ARRAYS>(a, tiles);
+      } else if (q == 0) {
+        launch_pass<K, unsigned, false, IN_SRC, OUT_ARRAYS>(a, tiles);
+      } else if (!final) {
+        launch_pass<K, unsigned, false, IN_ARRAYS, OUT_ARRAYS>(a, tiles);
+      } else if (direct) {
+        launch_pass<K, unsigned, false, IN_ARRAYS, OUT_RANK>(a, tiles);
+      } else {
+        launch_pass<K, unsigned, false, IN_ARRAYS, OUT_PAIRS>(a, tiles);
+      }
     } else {
       // segment passes: the segment number is the key, indices ride along
-      PassArgs<unsigned> a{};
+      PassArgs<unsigned, unsigned> a{};
       const bool first_seg = (q == key_passes);
-      a.kin = first_seg ? aA : (const unsigned *)kA; a.iin = iA; a.ain = nullptr;
-      a.kout = (unsigned *)kB; a.iout = iB; a.aout = nullptr;
-      a.rank = (int *)d; a.segoff = segoff;
+      a.kin = first_seg ? aA : (const unsigned *)kA; a.vin = iA; a.ain = nullptr;
+      a.kout = (unsigned *)kB; a.vout = iB; a.aout = nullptr;
+      a.rank = (int *)d; a.segoff = segoff; a.pidx = pidx; a.ppos = ppos;
       a.starts = hist + q * 256; a.state = state; a.counter = counters + q;
       a.n = n; a.shift = 8 * (q - key_passes); a.status = S.d_status; a.spin_limit = S.spin_limit;
-      if (final) launch_pass<unsigned, false, true>(a, tiles);
-      else launch_pass<unsigned, false, false>(a, tiles);
+      if (!final) launch_pass<unsigned, unsigned, false, IN_ARRAYS, OUT_ARRAYS>(a, tiles);
+      else if (direct) launch_pass<unsigned, unsigned, false, IN_ARRAYS, OUT_RANK>(a, tiles);
+      else launch_pass<unsigned, unsigned, false, IN_ARRAYS, OUT_PAIRS>(a, tiles);
     }
     if (!final) {
       std::swap(kA, kB); std::swap(iA, iB);
       if (keypass) std::swap(aA, aB);
     }
+  }
+  if (!direct) {
+    // (index, position) pairs in sorted order -> windows of the index ->
+    // rank[index] = position, one window at a time
+    const int shift = window_shift(n);
+    unsigned *wst = hist + RK_MAXPASS * 256;
+    k_window_starts<<<1, 256, 0, S.stream>>>(wst, n, shift);
+    launch_check("k_window_starts");
+    GCVL_CK(cudaMemsetAsync(state, 0, rk_state_bytes(n), S.stream));
+    PassArgs<unsigned, unsigned> a{};
+    a.kin = pidx; a.vin = ppos;
+    a.kout = iA; a.vout = (unsigned *)kA;  // free: the last pass read (kA, iA)
+    a.starts = wst; a.state = state; a.counter = counters + RK_MAXPASS;
+    a.n = n; a.shift = shift; a.status = S.d_status; a.spin_limit = S.spin_limit;
+    launch_pass<unsigned, unsigned, false, IN_ARRAYS, OUT_ARRAYS>(a, tiles);
+    const long g = ((long)n + RK_BLOCK * SC_ITEMS - 1) / (RK_BLOCK * SC_ITEMS);
+    k_window_scatter<unsigned><<<(int)g, RK_BLOCK, 0, S.stream>>>((unsigned *)d, iA, (const unsigned *)kA, n);
+    launch_check("k_window_scatter");
   }
 }
 

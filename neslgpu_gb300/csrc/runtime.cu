@@ -104,8 +104,9 @@ GCVL_EXPORT int gcvl_sync(void) {
   if (!GCVL_CK(cudaStreamSynchronize(s.stream))) return s.err;
   unsigned word = 0;
   if (!GCVL_CK(cudaMemcpy(&word, s.d_status, 4, cudaMemcpyDeviceToHost))) return s.err;
-  if (word & DEV_TIMEOUT) {
-    set_error(GCVL_ERR_TIMEOUT, "a bounded device wait gave up (status 0x%x)", word);
+  if (word & DEV_TIMEOUT) set_error(GCVL_ERR_TIMEOUT, "a bounded device wait gave up (status 0x%x)", word);
+  if (word & DEV_RANGE) set_error(GCVL_ERR_RANGE, "a kernel was given input outside its range and skipped it (status 0x%x)", word);
+  if (word) {
     unsigned zero = 0;
     cudaMemcpy(s.d_status, &zero, 4, cudaMemcpyHostToDevice);
   }

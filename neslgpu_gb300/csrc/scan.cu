@@ -23,7 +23,6 @@ template <class T> struct Tiling;
 template <> struct Tiling<int> { static constexpr int BLOCK = 256, ITEMS = 16; };
 template <> struct Tiling<double> { static constexpr int BLOCK = 256, ITEMS = 8; };
 
-enum Mode { M_SCAN = 0, M_REDUCE = 1, M_OFFSETS = 2 };
 
 template <class T> struct ScanArgs {
   T *out;            // scan: n outputs; reduce: m outputs; offsets: m+1
@@ -305,27 +304,6 @@ template <int ITEMS> struct Engine<AddD, ITEMS> {
     tv = fx_to_double(acc, emax);  // never -0.0, so starting from init 0.0 changes nothing
   }
 };
-
-// Sum of x[from..to) by the fixed-point path (FP64 when inf/NaN present).
-template <int ITEMS>
-__device__ __forceinline__ double fx_range(const double (&x)[ITEMS], int from, int to) {
-  int emax = 1;
-#pragma unroll
-  for (int i = 0; i < ITEMS; i++)
-    if (i >= from && i < to) emax = max(emax, fx_exp((unsigned long long)__double_as_longlong(x[i])));
-  if (emax == 2047) {
-    double v = -0.0;
-#pragma unroll
-    for (int i = 0; i < ITEMS; i++)
-      if (i >= from && i < to) v = __dadd_rn(v, x[i]);
-    return v;
-  }
-  long long acc = 0;
-#pragma unroll
-  for (int i = 0; i < ITEMS; i++)
-    if (i >= from && i < to) fx_add(acc, (unsigned long long)__double_as_longlong(x[i]), emax);
-  return fx_to_double(acc, emax);
-}
 
 // The CTA has TT compute threads (one 128-byte row each) plus one look-back
 // warp.  The look-back warp issues the tile's TMA load and at once starts

@@ -53,6 +53,68 @@ template <class F> void each(F f, long n, const char *name) {
   launch_check(name);
 }
 
+// Unsegmented gather and scatter: PITEMS elements per thread with all their
+// index loads, then all their data accesses, in flight together (random
+// accesses are latency-bound; one element per thread leaves HBM idle).
+constexpr int GITEMS = 8;
+template <class T>
+__global__ void __launch_bounds__(VBLOCK) k_gather(T *__restrict__ d, const T *__restrict__ s,
+                                                   const int *__restrict__ idx, long n) {
+  const long i0 = (long)blockIdx.x * (VBLOCK * GITEMS) + threadIdx.x;
+  int ix[GITEMS];
+  T v[GITEMS];
+#pragma unroll
+  for (int u = 0; u < GITEMS; u++) {
+    const long i = i0 + (long)u * VBLOCK;
+    ix[u] = i < n ? __ldcs(idx + i) : 0;
+  }
+#pragma unroll
+  for (int u = 0; u < GITEMS; u++)
+    if (i0 + (long)u * VBLOCK < n) v[u] = __ldg(s + ix[u]);
+#pragma unroll
+  for (int u = 0; u < GITEMS; u++) {
+    const long i = i0 + (long)u * VBLOCK;
+    if (i < n) __stcs(d + i, v[u]);
+  }
+}
+template <class T>
+__global__ void __launch_bounds__(VBLOCK) k_scatter(T *__restrict__ d, const T *__restrict__ s,
+                                                    const int *__restrict__ idx, long n) {
+  const long i0 = (long)blockIdx.x * (VBLOCK * GITEMS) + threadIdx.x;
+  int ix[GITEMS];
+  T v[GITEMS];
+#pragma unroll
+  for (int u = 0; u < GITEMS; u++) {
+    const long i = i0 + (long)u * VBLOCK;
+    if (i < n) { ix[u] = __ldcs(idx + i); v[u] = __ldcs(s + i); }
+  }
+#pragma unroll
+  for (int u = 0; u < GITEMS; u++)
+    if (i0 + (long)u * VBLOCK < n) d[ix[u]] = v[u];
+}
+template <class T> void gather(T *d, const T *s, const int *idx, long n, const char *name) {
+  if (n <= 0) return;
+  k_gather<T><<<(int)((n + VBLOCK * GITEMS - 1) / (VBLOCK * GITEMS)), VBLOCK, 0, stream()>>>(d, s, idx, n);
+  launch_check(name);
+}
+// bit moves: int and cvl_bool as 32-bit words, double as 64-bit words
+template <class T> struct Bits { typedef unsigned type; };
+template <> struct Bits<double> { typedef unsigned long long type; };
+template <class T> void scatter(T *d, const T *s, const int *idx, int n, int n_d, vec_p scratch, const char *name) {
+  typedef typename Bits<T>::type U;
+  if (n <= 0) return;
+  if (scatter_partitioned_wanted(n_d, sizeof(T))) {
+    scatter_partitioned<U>((U *)d, (const U *)s, idx, n, n_d, scratch);
+    return;
+  }
+  k_scatter<T><<<(int)(((long)n + VBLOCK * GITEMS - 1) / (VBLOCK * GITEMS)), VBLOCK, 0, stream()>>>(d, s, idx, n);
+  launch_check(name);
+}
+template <class T> int scatter_units(int n, int n_d) {
+  if (n <= 0 || !scatter_partitioned_wanted(n_d, sizeof(T))) return 0;
+  return (int)((scatter_partitioned_bytes(n, sizeof(T)) + 7) / 8);
+}
+
 // ----------------------------------------------------------- functors ---
 template <class T> struct ExtSeg {  // d[g] = s[off[g] + i[g]]
   T *d; const T *s; const int *i; const int *off;
@@ -314,27 +376,29 @@ META_SEG(ind_lez, INPLACE_NONE)
 // ------------------------------------------------------------- permutes ---
 #define PERMS(L, T)                                                                     \
   GCVL_EXPORT void smp_pu##L(vec_p d, vec_p s, vec_p i, int len, vec_p scratch) {       \
-    (void)scratch; ensure_init();                                                       \
-    each(Perm<T>{(T *)d, (const T *)s, (const int *)i}, len, "smp_pu" #L);              \
+    ensure_init();                                                                      \
+    scatter<T>((T *)d, (const T *)s, (const int *)i, len, len, scratch, "smp_pu" #L);   \
   }                                                                                     \
-  META1(smp_pu##L, INPLACE_NONE)                                                        \
+  GCVL_EXPORT int smp_pu##L##_scratch(int len) { return scatter_units<T>(len, len); }   \
+  GCVL_EXPORT unsigned smp_pu##L##_inplace(void) { return INPLACE_NONE; }               \
   GCVL_EXPORT void smp_pe##L(vec_p d, vec_p s, vec_p i, vec_p sd, int n, int m,         \
                              vec_p scratch) {                                           \
-    (void)scratch; ensure_init();                                                       \
-    if (m == 1) { each(Perm<T>{(T *)d, (const T *)s, (const int *)i}, n, "smp_pe" #L); return; } \
+    ensure_init();                                                                      \
+    if (m == 1) { scatter<T>((T *)d, (const T *)s, (const int *)i, n, n, scratch, "smp_pe" #L); return; } \
     segwalk(PermSeg<T>{(T *)d, (const T *)s, (const int *)i}, seg_view(sd, n, m), "smp_pe" #L); \
   }                                                                                     \
-  META_SEG(smp_pe##L, INPLACE_NONE)                                                     \
+  GCVL_EXPORT int smp_pe##L##_scratch(int n, int m) { return m == 1 ? scatter_units<T>(n, n) : 0; } \
+  GCVL_EXPORT unsigned smp_pe##L##_inplace(void) { return INPLACE_NONE; }               \
   GCVL_EXPORT void bck_pu##L(vec_p d, vec_p s, vec_p i, int s_len, int d_len,           \
                              vec_p scratch) {                                           \
     (void)s_len; (void)scratch; ensure_init();                                          \
-    each(BPerm<T>{(T *)d, (const T *)s, (const int *)i}, d_len, "bck_pu" #L);           \
+    gather<T>((T *)d, (const T *)s, (const int *)i, d_len, "bck_pu" #L);                \
   }                                                                                     \
   META2(bck_pu##L, INPLACE_2)                                                           \
   GCVL_EXPORT void bck_pe##L(vec_p d, vec_p s, vec_p i, vec_p sd_s, int n_s, int m_s,   \
                              vec_p sd_d, int n_d, int m_d, vec_p scratch) {             \
     (void)scratch; ensure_init();                                                       \
-    if (m_s == 1) { each(BPerm<T>{(T *)d, (const T *)s, (const int *)i}, n_d, "bck_pe" #L); return; } \
+    if (m_s == 1) { gather<T>((T *)d, (const T *)s, (const int *)i, n_d, "bck_pe" #L); return; } \
     SegView ss = seg_view(sd_s, n_s, m_s);                                              \
     segwalk(BPermSeg<T>{(T *)d, (const T *)s, (const int *)i, ss.off, m_s},                 \
             seg_view(sd_d, n_d, m_d), "bck_pe" #L);                                     \
@@ -374,9 +438,12 @@ META_SEG(ind_lez, INPLACE_NONE)
                              int len_dest, vec_p scratch) {                             \
     ensure_init();                                                                      \
     copy_dev<T>(d, v, len_dest);                                                        \
-    smp_pu##L(d, s, i, len_src, scratch);                                               \
+    scatter<T>((T *)d, (const T *)s, (const int *)i, len_src, len_dest, scratch, "dpe_pu" #L); \
   }                                                                                     \
-  META2(dpe_pu##L, INPLACE_3)                                                           \
+  GCVL_EXPORT int dpe_pu##L##_scratch(int len_src, int len_dest) {                      \
+    return scatter_units<T>(len_src, len_dest);                                         \
+  }                                                                                     \
+  GCVL_EXPORT unsigned dpe_pu##L##_inplace(void) { return INPLACE_3; }                  \
   GCVL_EXPORT void dpe_pe##L(vec_p d, vec_p s, vec_p i, vec_p v, vec_p sd_s, int n_s,   \
                              int m_s, vec_p sd_d, int n_d, int m_d, vec_p scratch) {    \
     ensure_init();                                                                      \
@@ -386,7 +453,10 @@ META_SEG(ind_lez, INPLACE_NONE)
     segwalk(FPermSeg<T>{(T *)d, (const T *)s, (const int *)i, nullptr, sdd.off, m_d},   \
             seg_view(sd_s, n_s, m_s), "dpe_pe" #L);                                     \
   }                                                                                     \
-  META_SEG2(dpe_pe##L, INPLACE_3)                                                       \
+  GCVL_EXPORT int dpe_pe##L##_scratch(int n_s, int m_s, int n_d, int m_d) {             \
+    (void)m_d; return m_s == 1 ? scatter_units<T>(n_s, n_d) : 0;                        \
+  }                                                                                     \
+  GCVL_EXPORT unsigned dpe_pe##L##_inplace(void) { return INPLACE_3; }                  \
   GCVL_EXPORT void dfp_pu##L(vec_p d, vec_p s, vec_p i, vec_p f, vec_p v, int len_src,  \
                              int len_dest, vec_p scratch) {                             \
     ensure_init();                                                                      \

@@ -255,7 +255,8 @@ def smp_u(R, name, x, idx):
     n = len(x)
     a, ix = R.vec(x, k), R.vec(idx, "z")
     d = R.out(n, k)
-    R.fn(name)(R.p(d), R.p(a), R.p(ix), n, None)
+    scr = R.units(R.fn(name + "_scratch")(n))
+    R.fn(name)(R.p(d), R.p(a), R.p(ix), n, R.p(scr))
     r = R.get(d, n)
     R.done()
     return r
@@ -266,7 +267,8 @@ def smp_e(R, name, x, idx, lengths):
     sd, n, m = R.segd(lengths)
     a, ix = R.vec(x, k), R.vec(idx, "z")
     d = R.out(n, k)
-    R.fn(name)(R.p(d), R.p(a), R.p(ix), R.p(sd), n, m, None)
+    scr = R.units(R.fn(name + "_scratch")(n, m))
+    R.fn(name)(R.p(d), R.p(a), R.p(ix), R.p(sd), n, m, R.p(scr))
     r = R.get(d, n)
     R.done()
     return r
@@ -342,7 +344,8 @@ def dpe_u(R, name, x, idx, default):
     k = _kind(name)
     a, ix = R.vec(x, k), R.vec(idx, "z")
     d, v = R.vec(default, k), R.vec(default, k)
-    R.fn(name)(R.p(d), R.p(a), R.p(ix), R.p(v), len(x), len(default), None)
+    scr = R.units(R.fn(name + "_scratch")(len(x), len(default)))
+    R.fn(name)(R.p(d), R.p(a), R.p(ix), R.p(v), len(x), len(default), R.p(scr))
     r = R.get(d, len(default))
     R.done()
     return r
@@ -354,7 +357,8 @@ def dpe_e(R, name, x, idx, default, len_s, len_d):
     sdd, nd, md = R.segd(len_d)
     a, ix = R.vec(x, k), R.vec(idx, "z")
     d, v = R.vec(default, k), R.vec(default, k)
-    R.fn(name)(R.p(d), R.p(a), R.p(ix), R.p(v), R.p(sds), ns, ms, R.p(sdd), nd, md, None)
+    scr = R.units(R.fn(name + "_scratch")(ns, ms, nd, md))
+    R.fn(name)(R.p(d), R.p(a), R.p(ix), R.p(v), R.p(sds), ns, ms, R.p(sdd), nd, md, R.p(scr))
     r = R.get(d, nd)
     R.done()
     return r
