@@ -270,6 +270,110 @@ def batched_suite(g, nvec=8192, total=1 << 27, seed=3):
     return res
 
 
+def dispatch_suite(g, count=512, hi=24, seed=2024):
+    """The learned dispatcher on a seeded sweep of synthetic descriptors
+    (uniform / geometric / power-law / bimodal lengths, totals 2^16..2^hi,
+    int32 / uint32 / float64, segmented scan / reduce / rank): every valid
+    kernel variant timed, the MLP trained on 80 % with the library's CUDA
+    training kernel, its picks on the other 20 % scored against the
+    autotuned optimum (regret) and against always running the default
+    kernel (speed-up)."""
+    from neslgpu_gb300 import dispatch as D
+    t0 = time.time()
+    insts, X = D.sweep(count, seed=seed, lo=16, hi=hi, cvl=g.c)
+    res = D.train(insts, X, seed=7, epochs=400, batch=128, cvl=g.c)
+    out = {"instances": count, "log2_total_range": [16, hi], "test_instances": res["instances"]}
+    for k in ("regret_mean", "regret_p90", "regret_total", "accuracy", "speedup_vs_plain",
+              "speedup_autotuned_vs_plain", "speedup_vs_plain_geomean", "train_seconds"):
+        out[k] = round(res[k], 4)
+    out["decision_overhead_ms"] = round(D.dispatch_overhead_ms(g.c, res["params"]), 4)
+    out["wall_seconds"] = round(time.time() - t0, 1)
+    return out
+
+
+def _vcode_sort(cvl, keys, sync):
+    """QSORT through the VCODE interpreter: (seconds with the keys on the
+    device, seconds end to end from host keys to host result, sorted keys,
+    VCODE ops run)."""
+    from neslgpu_gb300 import vcode as V, vcode_programs as P
+    it = V.Interpreter(P.qsort_program(), cvl, sync=sync)
+    try:
+        t0 = time.perf_counter()
+        lv = it.from_host("I", [len(keys)])
+        sd = it.segdes_from_lengths(lv)
+        it.drop(lv)
+        kv = it.from_host("I", keys)
+        sync()
+        t1 = time.perf_counter()
+        st = it.run("QSORT", [sd, kv])
+        sync()
+        t2 = time.perf_counter()
+        out = it.to_host(st[-1])
+        t3 = time.perf_counter()
+        return t2 - t1, t3 - t0, out, it.ops_run
+    finally:
+        it.free_all()
+
+
+def vinterp_suite(g, log2n=26, log2rows=22, seed=2026):
+    """The plain drop-in at scale through a VCODE interpreter: NESL
+    quicksort (this repository's flattened VCODE program) on 2^log2n
+    uniform int32 keys, and sparse matrix-vector product as a VCODE
+    program on 2^log2rows rows with power-law row lengths (alpha 2.1 on
+    [1, 2^16]), float64 values and x."""
+    from neslgpu_gb300 import vcode as V, vcode_programs as P
+    c = g.c
+    sync = lambda: c.gcvl_sync()  # noqa: E731
+    r = np.random.default_rng(seed)
+    n = 1 << log2n
+    keys = r.integers(-2 ** 31, 2 ** 31, size=n, dtype=np.int64).astype(np.int32)
+    _vcode_sort(c, keys[: 1 << 16], sync)  # warm-up: kernels loaded, heap classes touched
+    dev_s, e2e_s, out, ops = _vcode_sort(c, keys, sync)
+    ok = bool(np.all(out[1:] >= out[:-1])) and int(out.astype(np.int64).sum()) == int(keys.astype(np.int64).sum())
+    qs = {"n": n, "keys": "uniform int32, seeded", "seconds": round(dev_s, 4),
+          "mkeys_s": round(n / dev_s / 1e6, 2), "e2e_seconds": round(e2e_s, 4),
+          "e2e_mkeys_s": round(n / e2e_s / 1e6, 2), "vcode_ops": ops, "sorted": ok}
+    # sparse matrix-vector product
+    rows = 1 << log2rows
+    lens = np.minimum(r.zipf(2.1, size=rows), 1 << 16).astype(np.int32)
+    nnz = int(lens.sum(dtype=np.int64))
+    cols = r.integers(0, rows, size=nnz).astype(np.int32)
+    vals = r.standard_normal(nnz)
+    x = r.standard_normal(rows)
+    it = V.Interpreter(P.spmv_program(), c, sync=sync)
+    try:
+        lv = it.from_host("I", lens)
+        rsd = it.segdes_from_lengths(lv)
+        it.drop(lv)
+        args = [rsd, it.from_host("I", cols), it.from_host("F", vals), it.from_host("F", x)]
+        times = []
+        for rep in range(4):
+            for a in args:
+                a.ref += 1  # keep the inputs across runs
+            sync()
+            t0 = time.perf_counter()
+            st = it.run("SPMV", list(args))
+            sync()
+            times.append(time.perf_counter() - t0)
+            y = st[0]
+            if rep < 3:
+                it.drop(y)
+        yh = it.to_host(y)
+        it.drop(y)
+        for a in args:
+            it.drop(a)
+    finally:
+        it.free_all()
+    starts = np.cumsum(lens, dtype=np.int64) - lens
+    chk = np.array([np.dot(vals[s:s + l], x[cols[s:s + l]]) for s, l in zip(starts[:2000], lens[:2000])])
+    t = float(np.median(times[1:]))
+    spmv = {"rows": rows, "nnz": nnz, "row_nnz": "power law alpha 2.1 on [1, 2^16]", "seconds": round(t, 5),
+            "gflop_s": round(2 * nnz / t / 1e9, 2),
+            "alg_gbs": round((nnz * (4 + 8 + 8) + 8 * rows + 4 * rows) / t / 1e9, 1),
+            "first_rows_max_abs_err": float(np.max(np.abs(yh[:2000] - chk)))}
+    return {"quicksort": qs, "spmv": spmv}
+
+
 def cpu_baseline_port(x, lens, threads=1):
     """The oracle restatement of the serial CVL on this host: add_sed and
     add_red over the same values and segments.  With threads > 1 the
@@ -430,10 +534,12 @@ def gpu_arm(a):
         cpu["max_rel_diff_scan"] = float(np.max(np.abs(gs - scan) / np.maximum(np.abs(scan), 1.0)))
         cpu["max_rel_diff_reduce"] = float(np.max(np.abs(gr - red) / np.maximum(np.abs(red), 1.0)))
 
-    prims = batched = None
+    prims = batched = dispatch = vinterp = None
     if not a.no_suite and rank == 0:
         prims = primitive_suite(g, n, hbm)
         batched = batched_suite(g)
+        dispatch = dispatch_suite(g)
+        vinterp = vinterp_suite(g)
 
     if rank == 0:
         line = {
@@ -447,7 +553,8 @@ def gpu_arm(a):
                        "l2": "inputs larger than L2 (2 GiB per vector), no flush",
                        "parallelism": f"{world} independent replicas"},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
-            "clocks": clk.summary(w0, w1), "primitives": prims, "batched": batched,
+            "clocks": clk.summary(w0, w1), "primitives": prims, "batched": batched, "dispatch": dispatch,
+            "vinterp": vinterp,
         }
         print(json.dumps(line))
 
@@ -502,6 +609,10 @@ def main():
     ap.add_argument("--suite-only", action="store_true",
                     help="only the per-primitive table at 2^log2n (for profiling)")
     ap.add_argument("--batched-only", action="store_true", help="only the batched workload")
+    ap.add_argument("--dispatch-only", action="store_true", help="only the learned-dispatcher sweep")
+    ap.add_argument("--vinterp-only", action="store_true", help="only the VCODE programs")
+    ap.add_argument("--dispatch-count", type=int, default=4096)
+    ap.add_argument("--dispatch-hi", type=int, default=28)
     a = ap.parse_args()
     a.warmup = max(a.warmup, 3) if a.impl == "gb300" else a.warmup
     if a.impl == "reference":
@@ -512,6 +623,10 @@ def main():
         print(json.dumps({"primitives": primitive_suite(g, 1 << a.log2n, peaks()[0])}))
     elif a.batched_only:
         print(json.dumps({"batched": batched_suite(Gpu())}))
+    elif a.vinterp_only:
+        print(json.dumps({"vinterp": vinterp_suite(Gpu())}))
+    elif a.dispatch_only:
+        print(json.dumps({"dispatch": dispatch_suite(Gpu(), count=a.dispatch_count, hi=a.dispatch_hi)}))
     else:
         gpu_arm(a)
 

@@ -1,0 +1,636 @@
+"""A VCODE interpreter over the CVL C ABI -- the role vinterp plays for the
+reference (nesl/vcode/main.c, stack.c, vstack.c), written for this library.
+
+VCODE is the stack-machine language the NESL compiler emits: every value on
+the stack is a vector (a scalar is a vector of length 1) of INT, FLOAT or
+BOOL elements, or a segment descriptor; every vector operation is one CVL
+call.  The interpreter follows vinterp's conventions for the calls:
+
+* elementwise ops call ``*_wu*`` with the length of their first argument;
+* scans, reductions and ranks call the segmented form ``*_se*``/``*_re*``/
+  ``rk*_le*`` with the segment descriptor on top of the stack (an
+  unsegmented vector carries a one-segment descriptor);
+* PACK is ``pk1_lev`` + ``add_ruz`` + ``mke_fov`` + ``pk2_le*``, and
+  MAKE_SEGDES is ``add_ruz`` + ``mke_fov`` (main.c:510-641);
+* argument i of an op is the i-th of the top arg_count stack entries, the
+  deepest first (stack.c:361-376); results are pushed in order;
+* COPY c s / POP c s / CPOP c s copy, drop or move the c entries that sit s
+  below the top (stack.c:186-318);
+* IF pops a BOOL scalar (stack.c:124-142); scalars that steer control flow
+  are read back to the host, as in vinterp.
+
+What differs from vinterp, by design: memory comes from a size-class cache
+over ``alo_foz`` (one device allocation per size class and reuse, instead
+of one heap with compaction); constants are uploaded once and then shared;
+the same interpreter runs on any implementation of the ABI -- the GPU
+library or, for the parity tests and the CPU baseline, the oracle.
+"""
+from __future__ import annotations
+
+import re
+import time
+from dataclasses import dataclass
+
+import numpy as np
+
+from .cvl import CVL, check, load
+
+# ------------------------------------------------------------ op table ---
+TYPE_SUFFIX = {"INT": "z", "FLOAT": "d", "BOOL": "b"}
+KIND_OF = {"INT": "I", "FLOAT": "F", "BOOL": "B", "SEGDES": "S"}
+SUFFIX_OF_KIND = {"I": "z", "F": "d", "B": "b"}
+
+# elementwise: name -> (CVL stem, arity, result kind or None for "same as
+# argument 1", or "A2" for "same as argument 2")
+ELT = {
+    "+": ("add", 2, None), "-": ("sub", 2, None), "*": ("mul", 2, None), "/": ("div", 2, None),
+    "%": ("mod", 2, "I"), "<": ("les", 2, "B"), "<=": ("leq", 2, "B"), ">": ("grt", 2, "B"),
+    ">=": ("geq", 2, "B"), "=": ("eql", 2, "B"), "!=": ("neq", 2, "B"), "LSHIFT": ("lsh", 2, "I"),
+    "RSHIFT": ("rsh", 2, "I"), "NOT": ("not", 1, None), "AND": ("and", 2, None), "OR": ("ior", 2, None),
+    "XOR": ("xor", 2, None), "SELECT": ("sel", 3, "A2"), "RAND": ("rnd", 1, "I"),
+    "FLOOR": ("flr", 1, "I"), "CEIL": ("cei", 1, "I"), "TRUNC": ("trn", 1, "I"), "ROUND": ("rou", 1, "I"),
+    "LOG": ("log", 1, "F"), "SQRT": ("sqt", 1, "F"), "EXP": ("exp", 1, "F"), "SIN": ("sin", 1, "F"),
+    "COS": ("cos", 1, "F"), "TAN": ("tan", 1, "F"), "ASIN": ("asn", 1, "F"), "ACOS": ("acs", 1, "F"),
+    "ATAN": ("atn", 1, "F"), "SINH": ("snh", 1, "F"), "COSH": ("csh", 1, "F"), "TANH": ("tnh", 1, "F"),
+    "I_TO_F": ("dbl", 1, "F"), "I_TO_B": ("boo", 1, "B"), "B_TO_I": ("int", 1, "I"),
+}
+# the type an untyped elementwise op works on (grammar.yy:160-243)
+ELT_DEFAULT_TYPE = {"%": "INT", "LSHIFT": "INT", "RSHIFT": "INT", "RAND": "INT", "I_TO_F": "INT",
+                    "I_TO_B": "INT", "B_TO_I": "BOOL", "FLOOR": "FLOAT", "CEIL": "FLOAT", "TRUNC": "FLOAT",
+                    "ROUND": "FLOAT", "LOG": "FLOAT", "SQRT": "FLOAT", "EXP": "FLOAT", "SIN": "FLOAT",
+                    "COS": "FLOAT", "TAN": "FLOAT", "ASIN": "FLOAT", "ACOS": "FLOAT", "ATAN": "FLOAT",
+                    "SINH": "FLOAT", "COSH": "FLOAT", "TANH": "FLOAT"}
+SCAN = {"+_SCAN": "add", "*_SCAN": "mul", "MAX_SCAN": "max", "MIN_SCAN": "min", "AND_SCAN": "and",
+        "OR_SCAN": "ior", "XOR_SCAN": "xor"}
+REDUCE = {"+_REDUCE": "add", "*_REDUCE": "mul", "MAX_REDUCE": "max", "MIN_REDUCE": "min",
+          "AND_REDUCE": "and", "OR_REDUCE": "ior", "XOR_REDUCE": "xor"}
+VEC = {"PERMUTE", "DPERMUTE", "FPERMUTE", "BPERMUTE", "BFPERMUTE", "DFPERMUTE", "EXTRACT", "REPLACE",
+       "DIST", "INDEX", "RANK_UP", "RANK_DOWN", "PACK"}
+TYPES = {"INT", "FLOAT", "BOOL", "SEGDES", "CHAR"}
+STACK_OPS = {"COPY", "POP", "CPOP"}
+
+
+class VcodeError(RuntimeError):
+    pass
+
+
+# --------------------------------------------------------------- parse ---
+@dataclass
+class Ins:
+    op: str
+    typ: str | None = None
+    a: object = None   # COPY/POP/CPOP count; CALL target name; CONST value
+    b: object = None   # COPY/POP/CPOP depth; branch target
+    line: int = 0
+
+
+_TOKEN = re.compile(r"\{[^}]*\}|\(|\)|\"[^\"]*\"|[^\s(){}\"]+")
+
+
+def parse(text: str) -> tuple[list[Ins], dict[str, int], str]:
+    """VCODE text -> (instructions, function entry points, first function).
+    Grammar after nesl/vcode/grammar.yy: FUNC name [I types O types]
+    statements RET; comments in braces."""
+    toks = []
+    for lineno, line in enumerate(text.splitlines(), 1):
+        for t in _TOKEN.findall(line):
+            if not t.startswith("{"):
+                toks.append((t, lineno))
+    prog: list[Ins] = []
+    funcs: dict[str, int] = {}
+    first = None
+    i = 0
+    n = len(toks)
+    ifs: list[int] = []
+
+    def peek(k=0):
+        return toks[i + k][0] if i + k < n else None
+
+    while i < n:
+        t, ln = toks[i]
+        i += 1
+        if t == "FUNC":
+            name = toks[i][0]
+            i += 1
+            funcs[name] = len(prog)
+            first = first or name
+            if peek() == "I":  # input / output type declarations
+                i += 1
+                while peek() is not None and peek() != "O":
+                    i += 1
+                i += 1
+                while peek() in TYPES:
+                    i += 1
+            continue
+        if t in STACK_OPS:
+            prog.append(Ins(t, None, int(toks[i][0]), int(toks[i + 1][0]), ln))
+            i += 2
+        elif t == "CALL":
+            prog.append(Ins("CALL", None, toks[i][0], None, ln))
+            i += 1
+        elif t == "RET":
+            prog.append(Ins("RET", line=ln))
+        elif t == "IF":
+            ifs.append(len(prog))
+            prog.append(Ins("IF", line=ln))
+        elif t == "ELSE":
+            j = ifs.pop()
+            ifs.append(len(prog))
+            prog[j].b = len(prog) + 1  # IF false -> after ELSE
+            prog.append(Ins("ELSE", line=ln))
+        elif t == "ENDIF":
+            j = ifs.pop()
+            prog[j].b = len(prog)       # to here (IF false, or ELSE skipping the else-branch)
+            prog.append(Ins("ENDIF", line=ln))
+        elif t == "CONST":
+            typ = toks[i][0]
+            i += 1
+            if peek() == "(":
+                i += 1
+                vals = []
+                while peek() != ")":
+                    vals.append(toks[i][0])
+                    i += 1
+                i += 1
+                prog.append(Ins("CONSTV", typ, vals, None, ln))
+            else:
+                prog.append(Ins("CONST", typ, toks[i][0], None, ln))
+                i += 1
+        elif t in ("START_TIMER", "STOP_TIMER", "EXIT", "MAKE_SEGDES", "LENGTHS", "PAIR", "UNPAIR", "FOPEN",
+                   "FCLOSE", "FREAD_CHAR", "SPAWN"):
+            prog.append(Ins(t, line=ln))
+        elif t in ("SRAND", "READ", "WRITE", "FREAD", "FWRITE", "LENGTH") or t in ELT or t in SCAN or \
+                t in REDUCE or t in VEC:
+            typ = None
+            if peek() in TYPES:
+                typ = toks[i][0]
+                i += 1
+            prog.append(Ins(t, typ, line=ln))
+        else:
+            raise VcodeError(f"line {ln}: unknown token {t!r}")
+    # resolve calls
+    for ins in prog:
+        if ins.op == "CALL":
+            if ins.a not in funcs:
+                raise VcodeError(f"line {ins.line}: CALL of undefined {ins.a}")
+            ins.b = funcs[ins.a]
+    return prog, funcs, ("MAIN" if "MAIN" in funcs else first)
+
+
+# ---------------------------------------------------------------- values ---
+class Vec:
+    __slots__ = ("kind", "len", "seg_len", "ptr", "cls", "ref", "const")
+
+    def __init__(self, kind, length, seg_len, ptr, cls):
+        self.kind, self.len, self.seg_len, self.ptr, self.cls = kind, length, seg_len, ptr, cls
+        self.ref = 1
+        self.const = False
+
+    def __repr__(self):
+        return f"Vec({self.kind}, len={self.len}, seg_len={self.seg_len})"
+
+
+class Heap:
+    """Size-class cache over alo_foz: freed blocks wait for the next request
+    of their class instead of going back to the allocator."""
+
+    def __init__(self, c: CVL):
+        self.c = c
+        self.free: dict[int, list[int]] = {}
+        self.held = 0
+
+    @staticmethod
+    def size_class(units: int) -> int:
+        u = max(int(units), 4)
+        return 1 << (u - 1).bit_length()
+
+    def alloc(self, units: int) -> tuple[int, int]:
+        cls = self.size_class(units)
+        lst = self.free.get(cls)
+        if lst:
+            return lst.pop(), cls
+        p = self.c.alo_foz(cls)
+        if not p:
+            self.trim()
+            p = self.c.alo_foz(cls)
+            if not p:
+                raise MemoryError(f"alo_foz({cls}) failed")
+        self.held += cls
+        return p, cls
+
+    def release(self, ptr: int, cls: int):
+        self.free.setdefault(cls, []).append(ptr)
+
+    def trim(self):
+        for cls, lst in self.free.items():
+            for p in lst:
+                self.c.fre_fov(p)
+                self.held -= cls
+        self.free.clear()
+
+
+# ----------------------------------------------------------- interpreter ---
+class Interpreter:
+    """Runs a parsed VCODE program on one CVL implementation."""
+
+    def __init__(self, text: str, cvl: CVL | None = None, sync=None):
+        self.c = c = cvl or load()
+        self.prog, self.funcs, self.main = parse(text)
+        self.heap = Heap(c)
+        self.stack: list[Vec] = []
+        self.scratch_ptr, self.scratch_units = 0, 0
+        self._consts: dict = {}
+        self._scalar_cache: dict = {}
+        self.sync = sync or (lambda: None)
+        self.timer = 0.0
+        self.ops_run = 0
+        self._fn = {}
+
+    # -- memory
+    def fn(self, name):
+        f = self._fn.get(name)
+        if f is None:
+            f = self._fn[name] = getattr(self.c, name)
+        return f
+
+    def sfn(self, name):
+        """The F_scratch function of name; an implementation that allocates
+        its own temporaries (the oracle) has none, and needs no scratch."""
+        f = self._fn.get(name)
+        if f is None:
+            f = getattr(self.c, name, None) or (lambda *a: 0)
+            self._fn[name] = f
+        return f
+
+    def units(self, kind, length, seg_len=None):
+        c = self.c
+        if kind == "S":
+            return c.siz_fos(seg_len, length)
+        if kind == "F":
+            return c.siz_fod(max(length, 1))
+        return c.siz_foz(max(length, 1)) if kind == "I" else c.siz_fob(max(length, 1))
+
+    def new(self, kind, length, seg_len=None) -> Vec:
+        ptr, cls = self.heap.alloc(self.units(kind, length, seg_len))
+        return Vec(kind, length, seg_len if kind == "S" else None, ptr, cls)
+
+    def drop(self, v: Vec):
+        v.ref -= 1
+        if v.ref == 0 and not v.const:
+            self.heap.release(v.ptr, v.cls)
+
+    def scratch(self, units: int):
+        if units > self.scratch_units:
+            if self.scratch_ptr:
+                self.c.fre_fov(self.scratch_ptr)
+            self.scratch_units = max(int(units), 2 * self.scratch_units, 1024)
+            self.scratch_ptr = self.c.alo_foz(self.scratch_units)
+            if not self.scratch_ptr:
+                raise MemoryError("scratch")
+        return self.scratch_ptr
+
+    def free_all(self):
+        for v in self.stack:
+            self.drop(v)
+        self.stack.clear()
+        for v in list(self._consts.values()) + list(self._scalar_cache.values()):
+            v.const = False
+            v.ref = 1
+            self.drop(v)
+        self._consts.clear()
+        self._scalar_cache.clear()
+        self.heap.trim()
+        if self.scratch_ptr:
+            self.c.fre_fov(self.scratch_ptr)
+            self.scratch_ptr, self.scratch_units = 0, 0
+
+    # -- host <-> vector
+    def from_host(self, kind, arr) -> Vec:
+        a = np.ascontiguousarray(arr, dtype=np.float64 if kind == "F" else np.int32)
+        v = self.new(kind, len(a))
+        if len(a):
+            self.fn("c2v_fud" if kind == "F" else ("c2v_fuz" if kind == "I" else "c2v_fub"))(
+                v.ptr, a.ctypes.data, len(a), None)
+        return v
+
+    def to_host(self, v: Vec) -> np.ndarray:
+        if v.kind == "S":
+            out = np.empty(v.len, dtype=np.int32)
+            lv = self.new("I", v.len)
+            if v.len:
+                self.fn("len_fos")(lv.ptr, v.ptr, v.seg_len, v.len, self.scratch(self.sfn("len_fos_scratch")(
+                    v.seg_len, v.len)))
+                self.fn("v2c_fuz")(out.ctypes.data, lv.ptr, v.len, None)
+            self.drop(lv)
+            return out
+        out = np.empty(v.len, dtype=np.float64 if v.kind == "F" else np.int32)
+        if v.len:
+            self.fn("v2c_fud" if v.kind == "F" else ("v2c_fuz" if v.kind == "I" else "v2c_fub"))(
+                out.ctypes.data, v.ptr, v.len, None)
+        return out
+
+    def scalar_int(self, v: Vec) -> int:
+        return int(self.fn("ext_vuz")(v.ptr, 0, 1, None))
+
+    def scalar_bool(self, v: Vec) -> bool:
+        return bool(self.fn("ext_vub")(v.ptr, 0, 1, None))
+
+    def const_scalar(self, kind, value) -> Vec:
+        key = (kind, value)
+        v = self._scalar_cache.get(key)
+        if v is None:
+            v = self.new(kind, 1)
+            if kind == "I":
+                self.fn("rep_vuz")(v.ptr, 0, int(value), 1, None)
+            elif kind == "F":
+                self.fn("rep_vud")(v.ptr, 0, float(value), 1, None)
+            else:
+                self.fn("rep_vub")(v.ptr, 0, 1 if value else 0, 1, None)
+            v.const = True
+            self._scalar_cache[key] = v
+        v.ref += 1
+        return v
+
+    def segdes_from_lengths(self, lens: Vec) -> Vec:
+        c = self.c
+        m = lens.len
+        n = int(self.fn("add_ruz")(lens.ptr, m, self.scratch(self.sfn("add_ruz_scratch")(m)))) if m else 0
+        sd = self.new("S", m, n)
+        self.fn("mke_fov")(sd.ptr, lens.ptr, n, m, self.scratch(self.sfn("mke_fov_scratch")(n, m)))
+        return sd
+
+    # -- main loop
+    def run(self, entry: str | None = None, args: list[Vec] | None = None) -> list[Vec]:
+        """Runs from `entry` (default: MAIN or the first function) with
+        `args` pushed; returns the final stack (the caller owns it)."""
+        prog = self.prog
+        self.stack = list(args or [])
+        st = self.stack
+        pc = self.funcs[entry or self.main]
+        rstack = [-1]
+        t_start = None
+        while pc >= 0:
+            ins = prog[pc]
+            op = ins.op
+            pc += 1
+            self.ops_run += 1
+            if op == "COPY":
+                k, d = ins.a, ins.b
+                seg = st[len(st) - d - k: len(st) - d]
+                for v in seg:
+                    v.ref += 1
+                st.extend(seg)
+            elif op == "CPOP":
+                k, d = ins.a, ins.b
+                lo, hi = len(st) - d - k, len(st) - d
+                seg = st[lo:hi]
+                del st[lo:hi]
+                st.extend(seg)
+            elif op == "POP":
+                k, d = ins.a, ins.b
+                lo, hi = len(st) - d - k, len(st) - d
+                for v in st[lo:hi]:
+                    self.drop(v)
+                del st[lo:hi]
+            elif op == "CALL":
+                rstack.append(pc)
+                pc = ins.b
+            elif op == "RET":
+                pc = rstack.pop()
+            elif op == "IF":
+                f = st.pop()
+                taken = self.scalar_bool(f)
+                self.drop(f)
+                if not taken:
+                    pc = ins.b
+            elif op == "ELSE":  # end of the then-branch: skip the else-branch
+                pc = ins.b
+            elif op == "ENDIF":
+                pass
+            elif op == "CONST":
+                st.append(self._const(ins))
+            elif op == "CONSTV":
+                st.append(self._const_vec(ins))
+            elif op == "START_TIMER":
+                self.sync()
+                t_start = time.perf_counter()
+            elif op == "STOP_TIMER":
+                self.sync()
+                self.timer = time.perf_counter() - (t_start or time.perf_counter())
+                v = self.new("F", 1)
+                self.fn("rep_vud")(v.ptr, 0, self.timer, 1, None)
+                st.append(v)
+            elif op == "EXIT":
+                break
+            else:
+                self._vector_op(ins)
+        return self.stack
+
+    def _const(self, ins):
+        t = ins.typ
+        if t == "INT":
+            return self.const_scalar("I", int(ins.a))
+        if t == "FLOAT":
+            return self.const_scalar("F", float(ins.a))
+        if t == "BOOL":
+            return self.const_scalar("B", ins.a in ("T", "1"))
+        if t == "SEGDES":  # one segment of the given length
+            key = ("S", int(ins.a))
+            v = self._consts.get(key)
+            if v is None:
+                lens = self.from_host("I", [int(ins.a)])
+                v = self.segdes_from_lengths(lens)
+                self.drop(lens)
+                v.const = True
+                self._consts[key] = v
+            v.ref += 1
+            return v
+        raise VcodeError(f"line {ins.line}: CONST of type {t}")
+
+    def _const_vec(self, ins):
+        key = id(ins)
+        v = self._consts.get(key)
+        if v is None:
+            t = ins.typ
+            if t == "FLOAT":
+                v = self.from_host("F", [float(x) for x in ins.a])
+            elif t == "BOOL":
+                v = self.from_host("B", [1 if x == "T" else 0 for x in ins.a])
+            elif t == "SEGDES":
+                lens = self.from_host("I", [int(x) for x in ins.a])
+                v = self.segdes_from_lengths(lens)
+                self.drop(lens)
+            else:
+                v = self.from_host("I", [int(x) for x in ins.a])
+            v.const = True
+            self._consts[key] = v
+        v.ref += 1
+        return v
+
+    # -- vector operations
+    def _vector_op(self, ins):
+        op, st = ins.op, self.stack
+        if op in ELT:
+            stem, ar, res = ELT[op]
+            t = ins.typ or ELT_DEFAULT_TYPE.get(op) or "INT"
+            args = st[-ar:]
+            a0 = args[0]
+            kind = a0.kind if res is None else (args[1].kind if res == "A2" else res)
+            L = a0.seg_len if a0.kind == "S" else a0.len
+            d = self.new(kind, L)
+            name = f"{stem}_wu{TYPE_SUFFIX[t]}"
+            scr = self.scratch(self.sfn(name + "_scratch")(L))
+            self.fn(name)(d.ptr, *[a.ptr for a in args], L, scr)
+            self._finish(ar, [d])
+        elif op in SCAN or op in REDUCE or op in ("RANK_UP", "RANK_DOWN"):
+            t = TYPE_SUFFIX[ins.typ or "INT"]
+            x, sd = st[-2], st[-1]
+            if op in SCAN:
+                name, kind, L = f"{SCAN[op]}_se{t}", x.kind, x.len
+            elif op in REDUCE:
+                name, kind, L = f"{REDUCE[op]}_re{t}", x.kind, sd.len
+            else:
+                name, kind, L = ("rku_le" if op == "RANK_UP" else "rkd_le") + t, "I", x.len
+            d = self.new(kind, L)
+            scr = self.scratch(self.sfn(name + "_scratch")(sd.seg_len, sd.len))
+            self.fn(name)(d.ptr, x.ptr, sd.ptr, sd.seg_len, sd.len, scr)
+            self._finish(2, [d])
+        elif op == "MAKE_SEGDES":
+            lens = st[-1]
+            sd = self.segdes_from_lengths(lens)
+            self._finish(1, [sd])
+        elif op == "LENGTHS":
+            sd = st[-1]
+            d = self.new("I", sd.len)
+            self.fn("len_fos")(d.ptr, sd.ptr, sd.seg_len, sd.len,
+                               self.scratch(self.sfn("len_fos_scratch")(sd.seg_len, sd.len)))
+            self._finish(1, [d])
+        elif op == "LENGTH":
+            v = st[-1]
+            self._finish(1, [self.const_scalar("I", v.seg_len if v.kind == "S" else v.len)])
+        elif op == "PACK":
+            self._pack(ins)
+        elif op == "DIST":
+            t = TYPE_SUFFIX[ins.typ or "INT"]
+            v, sd = st[-2], st[-1]
+            d = self.new(v.kind, sd.seg_len)
+            name = f"dis_ve{t}"
+            self.fn(name)(d.ptr, v.ptr, sd.ptr, sd.seg_len, sd.len,
+                          self.scratch(self.sfn(name + "_scratch")(sd.seg_len, sd.len)))
+            self._finish(2, [d])
+        elif op == "INDEX":
+            init, stride, sd = st[-3], st[-2], st[-1]
+            d = self.new("I", sd.seg_len)
+            self.fn("ind_lez")(d.ptr, init.ptr, stride.ptr, sd.ptr, sd.seg_len, sd.len,
+                               self.scratch(self.sfn("ind_lez_scratch")(sd.seg_len, sd.len)))
+            self._finish(3, [d])
+        elif op == "EXTRACT":
+            t = TYPE_SUFFIX[ins.typ or "INT"]
+            x, idx, sd = st[-3], st[-2], st[-1]
+            d = self.new(x.kind, idx.len)
+            name = f"ext_ve{t}"
+            self.fn(name)(d.ptr, x.ptr, idx.ptr, sd.ptr, sd.seg_len, sd.len,
+                          self.scratch(self.sfn(name + "_scratch")(sd.seg_len, sd.len)))
+            self._finish(3, [d])
+        elif op == "REPLACE":
+            t = TYPE_SUFFIX[ins.typ or "INT"]
+            x, idx, val, sd = st[-4], st[-3], st[-2], st[-1]
+            if x.ref == 1 and not x.const:  # the only reference: replace in place
+                x.ref += 1
+                d = x
+            else:
+                d = self.new(x.kind, x.len)
+                cp = f"cpy_wu{t}"
+                self.fn(cp)(d.ptr, x.ptr, x.len, self.scratch(self.sfn(cp + "_scratch")(x.len)))
+            name = f"rep_ve{t}"
+            self.fn(name)(d.ptr, idx.ptr, val.ptr, sd.ptr, sd.seg_len, sd.len,
+                          self.scratch(self.sfn(name + "_scratch")(sd.seg_len, sd.len)))
+            self._finish(4, [d])
+        elif op == "PERMUTE":
+            t = TYPE_SUFFIX[ins.typ or "INT"]
+            x, idx, sd = st[-3], st[-2], st[-1]
+            d = self.new(x.kind, x.len)
+            name = f"smp_pe{t}"
+            self.fn(name)(d.ptr, x.ptr, idx.ptr, sd.ptr, sd.seg_len, sd.len,
+                          self.scratch(self.sfn(name + "_scratch")(sd.seg_len, sd.len)))
+            self._finish(3, [d])
+        elif op == "BPERMUTE":
+            t = TYPE_SUFFIX[ins.typ or "INT"]
+            x, idx, sds, sdd = st[-4], st[-3], st[-2], st[-1]
+            d = self.new(x.kind, idx.len)
+            name = f"bck_pe{t}"
+            self.fn(name)(d.ptr, x.ptr, idx.ptr, sds.ptr, sds.seg_len, sds.len, sdd.ptr, sdd.seg_len, sdd.len,
+                          self.scratch(self.sfn(name + "_scratch")(sds.seg_len, sds.len, sdd.seg_len, sdd.len)))
+            self._finish(4, [d])
+        elif op == "DPERMUTE":
+            t = TYPE_SUFFIX[ins.typ or "INT"]
+            x, idx, dflt, sds, sdd = st[-5], st[-4], st[-3], st[-2], st[-1]
+            if dflt.ref == 1 and not dflt.const:  # the default dies here: permute into it
+                dflt.ref += 1
+                d = dflt
+            else:
+                d = self.new(x.kind, dflt.len)
+            name = f"dpe_pe{t}"
+            self.fn(name)(d.ptr, x.ptr, idx.ptr, dflt.ptr, sds.ptr, sds.seg_len, sds.len, sdd.ptr, sdd.seg_len,
+                          sdd.len,
+                          self.scratch(self.sfn(name + "_scratch")(sds.seg_len, sds.len, sdd.seg_len, sdd.len)))
+            self._finish(5, [d])
+        elif op in ("FPERMUTE", "BFPERMUTE"):
+            t = TYPE_SUFFIX[ins.typ or "INT"]
+            x, idx, flg, sds, sdd = st[-5], st[-4], st[-3], st[-2], st[-1]
+            d = self.new(x.kind, sdd.seg_len)
+            name = ("fpm_pe" if op == "FPERMUTE" else "bfp_pe") + t
+            self.fn(name)(d.ptr, x.ptr, idx.ptr, flg.ptr, sds.ptr, sds.seg_len, sds.len, sdd.ptr, sdd.seg_len,
+                          sdd.len,
+                          self.scratch(self.sfn(name + "_scratch")(sds.seg_len, sds.len, sdd.seg_len, sdd.len)))
+            self._finish(5, [d])
+        elif op == "DFPERMUTE":
+            t = TYPE_SUFFIX[ins.typ or "INT"]
+            x, idx, flg, dflt, sds, sdd = st[-6:]
+            d = self.new(x.kind, dflt.len)
+            name = f"dfp_pe{t}"
+            self.fn(name)(d.ptr, x.ptr, idx.ptr, flg.ptr, dflt.ptr, sds.ptr, sds.seg_len, sds.len, sdd.ptr,
+                          sdd.seg_len, sdd.len,
+                          self.scratch(self.sfn(name + "_scratch")(sds.seg_len, sds.len, sdd.seg_len, sdd.len)))
+            self._finish(6, [d])
+        elif op == "SRAND":
+            s = st[-1]
+            self.fn("rnd_foz")(self.scalar_int(s))
+            self._finish(1, [self.const_scalar("B", True)])
+        elif op == "WRITE":
+            v = st.pop()
+            print(self.to_host(v))
+            self.drop(v)
+            st.append(self.new("I", 0))
+            st.append(self.const_scalar("B", True))
+        else:
+            raise VcodeError(f"line {ins.line}: {op} is not supported")
+
+    def _finish(self, nargs, results):
+        st = self.stack
+        for v in st[len(st) - nargs:]:
+            self.drop(v)
+        del st[len(st) - nargs:]
+        st.extend(results)
+
+    def _pack(self, ins):
+        st = self.stack
+        t = TYPE_SUFFIX[ins.typ or "INT"]
+        x, flg, sd = st[-3], st[-2], st[-1]
+        n, m = sd.seg_len, sd.len
+        lens = self.new("I", m)
+        self.fn("pk1_lev")(lens.ptr, flg.ptr, sd.ptr, n, m, self.scratch(self.sfn("pk1_lev_scratch")(n, m)))
+        dsd = self.segdes_from_lengths(lens)
+        self.drop(lens)
+        d = self.new(x.kind, dsd.seg_len)
+        name = f"pk2_le{t}"
+        self.fn(name)(d.ptr, x.ptr, flg.ptr, sd.ptr, n, m, dsd.ptr, dsd.seg_len, m,
+                      self.scratch(self.sfn(name + "_scratch")(n, m, dsd.seg_len, m)))
+        self._finish(3, [d, dsd])
+
+
+def run_program(text: str, cvl: CVL | None = None, entry: str | None = None, args=None, sync=None):
+    """Parses and runs; returns (interpreter, final stack)."""
+    it = Interpreter(text, cvl, sync=sync)
+    out = it.run(entry, args)
+    return it, out

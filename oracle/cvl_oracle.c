@@ -407,6 +407,22 @@ EXPORT void ocvl_len_fos(vec_p l, vec_p sd, int n, int m, vec_p scr) {
   (void)n; (void)scr; if (sd != l) memmove(l, sd, (size_t)m * sizeof(int));
 }
 
+/* Vector memory and host transfers (facilt.c:149-160, 252-283): malloc'd
+ * units of UNIT bytes, and element copies to and from host arrays.  Used by
+ * the VCODE interpreter when it runs on the oracle. */
+EXPORT vec_p ocvl_alo_foz(int size) { return malloc((size_t)(size > 0 ? size : 1) * UNIT); }
+EXPORT void ocvl_fre_fov(vec_p p) { free(p); }
+#define XFER(L, T)                                                                      \
+  EXPORT void ocvl_v2c_fu##L(void *d, vec_p s, int len, vec_p scr) {                    \
+    (void)scr; if (len > 0) memcpy(d, s, (size_t)len * sizeof(T));                      \
+  }                                                                                     \
+  EXPORT void ocvl_c2v_fu##L(vec_p d, void *s, int len, vec_p scr) {                    \
+    (void)scr; if (len > 0) memcpy(d, s, (size_t)len * sizeof(T));                      \
+  }
+XFER(z, int)
+XFER(b, cvl_bool)
+XFER(d, double)
+
 /* ============================ library (library.c) ======================= */
 EXPORT void ocvl_ind_luz(vec_p d, int init, int stride, int count, vec_p scr) {
   int *o = (int *)d; int cur = init; (void)scr;
