@@ -315,7 +315,7 @@ def _vcode_sort(cvl, keys, sync):
         it.free_all()
 
 
-def vinterp_suite(g, log2n=26, log2rows=22, seed=2026):
+def vinterp_suite(g, log2n=26, log2rows=22, seed=2026, cpu_sample_log2n=20):
     """The plain drop-in at scale through a VCODE interpreter: NESL
     quicksort (this repository's flattened VCODE program) on 2^log2n
     uniform int32 keys, and sparse matrix-vector product as a VCODE
@@ -333,6 +333,15 @@ def vinterp_suite(g, log2n=26, log2rows=22, seed=2026):
     qs = {"n": n, "keys": "uniform int32, seeded", "seconds": round(dev_s, 4),
           "mkeys_s": round(n / dev_s / 1e6, 2), "e2e_seconds": round(e2e_s, 4),
           "e2e_mkeys_s": round(n / e2e_s / 1e6, 2), "vcode_ops": ops, "sorted": ok}
+    if cpu_sample_log2n:
+        # the same interpreter and program on the oracle's serial CVL
+        # restatement, one host thread, on a bounded sample
+        from oracle.oracle import load_oracle
+        ns = 1 << cpu_sample_log2n
+        cs, _, cout, _ = _vcode_sort(load_oracle(), keys[:ns], lambda: None)
+        qs["cpu_baseline"] = {"mkeys_s": round(ns / cs / 1e6, 3), "n": ns, "cores": 1, "kind": "port",
+                              "sample": f"the first 2^{cpu_sample_log2n} keys, same VCODE program, oracle CVL",
+                              "sorted": bool(np.all(cout[1:] >= cout[:-1]))}
     # sparse matrix-vector product
     rows = 1 << log2rows
     lens = np.minimum(r.zipf(2.1, size=rows), 1 << 16).astype(np.int32)
@@ -364,13 +373,41 @@ def vinterp_suite(g, log2n=26, log2rows=22, seed=2026):
             it.drop(a)
     finally:
         it.free_all()
+    # the same product by the fused kernel (one launch, no intermediates)
+    lv_d = g.alloc(c.siz_foz(rows))
+    c.c2v_fuz(lv_d, lens.ctypes.data, rows, None)
+    sd_d = g.alloc(c.siz_fos(nnz, rows))
+    scr = g.alloc(max(c.mke_fov_scratch(nnz, rows), c.gcvl_spmv_csr_scratch(nnz, rows)))
+    c.mke_fov(sd_d, lv_d, nnz, rows, scr)
+    cols_d, vals_d, x_d, y_d = g.alloc(c.siz_foz(nnz)), g.alloc(c.siz_fod(nnz)), g.alloc(c.siz_fod(rows)), \
+        g.alloc(c.siz_fod(rows))
+    c.c2v_fuz(cols_d, cols.ctypes.data, nnz, None)
+    c.c2v_fud(vals_d, vals.ctypes.data, nnz, None)
+    c.c2v_fud(x_d, x.ctypes.data, rows, None)
+    ev = g.events(2)
+    ft = []
+    for rep in range(6):
+        c.gcvl_event_record(ev[0])
+        c.gcvl_spmv_csr(y_d, vals_d, cols_d, x_d, sd_d, nnz, rows, scr)
+        c.gcvl_event_record(ev[1])
+        ft.append(g.ms(ev[0], ev[1]) * 1e-3)
+    yf = np.empty(rows)
+    c.v2c_fud(yf.ctypes.data, y_d, rows, None)
+    g.check(c)
+    for p in (lv_d, sd_d, scr, cols_d, vals_d, x_d, y_d):
+        c.fre_fov(p)
+    tf = float(np.median(ft[1:]))
     starts = np.cumsum(lens, dtype=np.int64) - lens
     chk = np.array([np.dot(vals[s:s + l], x[cols[s:s + l]]) for s, l in zip(starts[:2000], lens[:2000])])
     t = float(np.median(times[1:]))
     spmv = {"rows": rows, "nnz": nnz, "row_nnz": "power law alpha 2.1 on [1, 2^16]", "seconds": round(t, 5),
             "gflop_s": round(2 * nnz / t / 1e9, 2),
             "alg_gbs": round((nnz * (4 + 8 + 8) + 8 * rows + 4 * rows) / t / 1e9, 1),
-            "first_rows_max_abs_err": float(np.max(np.abs(yh[:2000] - chk)))}
+            "first_rows_max_abs_err": float(np.max(np.abs(yh[:2000] - chk))),
+            "fused": {"kernel": "gcvl_spmv_csr", "seconds": round(tf, 6), "gflop_s": round(2 * nnz / tf / 1e9, 2),
+                      "alg_gbs": round((nnz * (4 + 8 + 8) + 8 * rows + 4 * rows) / tf / 1e9, 1),
+                      "speedup_vs_vcode": round(t / tf, 2),
+                      "max_abs_diff_vs_vcode": float(np.max(np.abs(yf - yh)))}}
     return {"quicksort": qs, "spmv": spmv}
 
 

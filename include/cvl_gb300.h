@@ -821,6 +821,14 @@ int gcvl_mlp_infer(const float *params, const float *X, int N, int *cls_dev);
 int gcvl_dispatch_set_model(const float *params_host);
 int gcvl_dispatch_choice(const char *prim, vec_p sd, int n, int m);
 int gcvl_auto_run(const char *prim, vec_p d, vec_p s, vec_p sd, int n, int m, vec_p scratch);
+/* Sparse matrix-vector product in one pass (no counterpart in the
+ * reference): y[r] = sum of vals[k] * x[cols[k]] over row r, rows given by
+ * the segment descriptor sd (rows segments over nnz elements).  The same
+ * products as BPERMUTE, * and +_REDUCE on FLOAT vectors compute, summed per
+ * row (float64 sums within the library's tolerance); empty rows give 0.
+ * Scratch: gcvl_spmv_csr_scratch(nnz, rows) units. */
+void gcvl_spmv_csr(vec_p y, vec_p vals, vec_p cols, vec_p x, vec_p sd, int nnz, int rows, vec_p scratch);
+int gcvl_spmv_csr_scratch(int nnz, int rows);
 /* The 48-bit lrand48 state behind rnd_wuz. */
 unsigned long long gcvl_rand_state(void);
 void gcvl_set_rand_state(unsigned long long state);

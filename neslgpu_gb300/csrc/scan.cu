@@ -34,6 +34,8 @@ template <class T> struct ScanArgs {
   unsigned *status;
   int spin_limit;
   int count_flags;   // pk1_lev: fold (x != 0) instead of x
+  const int *gidx;   // gather-multiply form: element k is in[k] * gsrc[gidx[k]]
+  const T *gsrc;
 };
 
 // Coalesced load of a tile into per-thread blocked registers through padded
@@ -98,7 +100,7 @@ __device__ __forceinline__ unsigned head_bits(const SegView &sv, int k0, int cnt
   return h;
 }
 
-template <class Op, int MODE, bool SEG>
+template <class Op, int MODE, bool SEG, bool GATHER = false>
 __global__ void __launch_bounds__(Tiling<typename Op::T>::BLOCK)
 k_scan(ScanArgs<typename Op::T> a) {
   typedef typename Op::T T;
@@ -106,6 +108,7 @@ k_scan(ScanArgs<typename Op::T> a) {
   constexpr int NW = BLOCK / 32;
   constexpr int PE = 128 / sizeof(T);
   __shared__ T s_stage[TILE + TILE / PE];
+  __shared__ int s_gidx[GATHER ? TILE + TILE / 32 : 1];
   __shared__ int s_wf[NW];
   __shared__ T s_wv[NW];
   __shared__ T s_prefix;
@@ -120,6 +123,19 @@ k_scan(ScanArgs<typename Op::T> a) {
 
   T x[ITEMS];
   load_blocked<T, ITEMS>(x, a.in + base, valid, Op::ident(), s_stage);
+  if constexpr (GATHER) {
+    // fused gather-multiply: the element is in[k] * gsrc[gidx[k]] (the
+    // products a BPERMUTE and an elementwise * would have materialised)
+    int g[ITEMS];
+    load_blocked<int, ITEMS>(g, a.gidx + base, valid, 0, s_gidx);
+    const int kk = threadIdx.x * ITEMS;
+    T v[ITEMS];
+#pragma unroll
+    for (int i = 0; i < ITEMS; i++) v[i] = (kk + i < valid) ? __ldg(a.gsrc + g[i]) : (T)1;
+#pragma unroll
+    for (int i = 0; i < ITEMS; i++)
+      if (kk + i < valid) x[i] = x[i] * v[i];
+  }
   if (a.count_flags) {
 #pragma unroll
     for (int i = 0; i < ITEMS; i++) x[i] = (x[i] != (T)0) ? (T)1 : (T)0;
@@ -645,6 +661,34 @@ void run_scan(typename Op::T *out, const typename Op::T *in, typename Op::T *out
   launch_check(name);
 }
 
+// Segmented sums of gathered products, y[r] = sum over row r of
+// vals[k] * x[cols[k]]: the BPERMUTE / * / +_REDUCE sequence of a sparse
+// matrix-vector product in one pass, without the two intermediate vectors.
+static void run_gather_mul_reduce(double *y, const double *vals, const int *cols, const double *x, vec_p sd,
+                                  int nnz, int rows, vec_p scratch) {
+  ensure_init();
+  State &S = st();
+  if (rows <= 0) return;
+  if (nnz <= 0) {
+    GCVL_CK(cudaMemsetAsync(y, 0, (size_t)rows * sizeof(double), S.stream));
+    return;
+  }
+  const int tiles = ceil_div(nnz, tile_elems<double>());
+  void *mem = scratch_or_work(scratch, lookback_bytes(tiles));
+  if (!mem) return;
+  ScanArgs<double> a{};
+  a.out = y; a.in = vals; a.out2 = nullptr; a.n = nnz;
+  a.sv = seg_view(sd, nnz, rows);
+  a.lb = lookback_carve(mem, tiles);
+  a.status = S.d_status;
+  a.spin_limit = S.spin_limit;
+  a.count_flags = 0;
+  a.gidx = cols; a.gsrc = x;
+  GCVL_CK(cudaMemsetAsync(mem, 0, lookback_clear_bytes(tiles), S.stream));
+  k_scan<AddD, M_REDUCE, true, true><<<tiles, Tiling<double>::BLOCK, 0, S.stream>>>(a);
+  launch_check("gcvl_spmv_csr");
+}
+
 // ---------------------------------------------- unsegmented reductions ---
 // Two-level reduction with a fixed combine order (deterministic for a given
 // device): per-CTA partials, then the last CTA folds them in CTA order.
@@ -998,3 +1042,15 @@ GCVL_EXPORT void gcvl_add_ruz_dev(vec_p d, vec_p s, int len, vec_p scratch) {
   run_reduce<AddZ>((const int *)s, len, (int *)d, scratch, false);
 }
 GCVL_EXPORT int gcvl_add_ruz_dev_scratch(int len) { return reduce_units<int>(len); }
+
+// y = A x for A in CSR form as CVL vectors: row descriptor sd (rows segments
+// over nnz), column indices cols and values vals (nnz each), x (ncols).
+GCVL_EXPORT void gcvl_spmv_csr(vec_p y, vec_p vals, vec_p cols, vec_p x, vec_p sd, int nnz, int rows,
+                               vec_p scratch) {
+  run_gather_mul_reduce((double *)y, (const double *)vals, (const int *)cols, (const double *)x, sd, nnz, rows,
+                        scratch);
+}
+GCVL_EXPORT int gcvl_spmv_csr_scratch(int nnz, int rows) {
+  (void)rows;
+  return lookback_units(ceil_div(nnz > 0 ? nnz : 1, tile_elems<double>()));
+}

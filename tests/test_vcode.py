@@ -111,3 +111,24 @@ def test_spmv_on_gpu(gpu, oracle):
     starts = np.cumsum(lens) - lens
     S = np.array([np.abs(vals[s:s + l] * x[cols[s:s + l]]).sum() for s, l in zip(starts, lens)])
     assert np.all(np.abs(got - want) <= 1e-12 * np.maximum(np.abs(want), S) + 1e-300)
+
+
+@pytest.mark.gpu
+def test_fused_spmv_matches_vcode_program(gpu, oracle):
+    """gcvl_spmv_csr (gather, multiply and per-row sum in one pass) against
+    the SPMV VCODE program on the oracle."""
+    from neslgpu_gb300.cvl import DeviceVector
+    c = gpu.cvl
+    lens, cols, vals, x = _csr(30_000, 7_000, 5)
+    want = _spmv(oracle.cvl, lens, cols, vals, x)
+    sd, nnz, rows = gpu.segd(lens)
+    cv, vv, xv = gpu.vec(cols, "z"), gpu.vec(vals, "d"), gpu.vec(x, "d")
+    y = gpu.out(rows, "d")
+    scr = gpu.units(c.gcvl_spmv_csr_scratch(nnz, rows))
+    c.gcvl_spmv_csr(y.ptr, vv.ptr, cv.ptr, xv.ptr, sd.ptr, nnz, rows, scr.ptr)
+    got = gpu.get(y, rows)
+    gpu.done()
+    starts = np.cumsum(lens) - lens
+    S = np.array([np.abs(vals[s:s + l] * x[cols[s:s + l]]).sum() for s, l in zip(starts, lens)])
+    assert np.all(np.abs(got - want) <= 1e-12 * np.maximum(np.abs(want), S) + 1e-300)
+    assert np.all(got[lens == 0] == 0.0)
