@@ -271,6 +271,7 @@ template <class T> struct TArgs {
   LookbackMem lb;
   unsigned *status;
   int spin_limit;
+  int *lead;  // reductions: per tile, the segment whose result lacks the earlier tiles' part (-1: none)
 };
 
 // Segment offsets seen through the shared-memory window when possible.
@@ -329,7 +330,7 @@ template <int ITEMS> struct Engine<AddD, ITEMS> {
 // exists and meet the look-back warp only when they need the carry.
 constexpr int TB_LB = TT + 32;  // threads per CTA
 template <class Op, int MODE, bool SEG>
-__global__ void __launch_bounds__(TB_LB, MODE == M_REDUCE ? 7 : 5) k_scan_tma(const __grid_constant__ CUtensorMap tin,
+__global__ void __launch_bounds__(TB_LB, MODE == M_REDUCE ? (sizeof(typename Op::T) == 8 ? 6 : 7) : 5) k_scan_tma(const __grid_constant__ CUtensorMap tin,
                                                      const __grid_constant__ CUtensorMap tout,
                                                      TArgs<typename Op::T> a) {
   typedef typename Op::T T;
@@ -360,14 +361,18 @@ __global__ void __launch_bounds__(TB_LB, MODE == M_REDUCE ? 7 : 5) k_scan_tma(co
 
   if (warp == NW) {
     // ------------------------------------------------------ look-back warp
-    bool first_head;
-    if (SEG) first_head = (__ldg(a.sv.bits + (base >> 5)) >> (base & 31)) & 1u;
-    else first_head = base == 0;
+    // (reductions do not wait: the one result per tile that needs earlier
+    // tiles' part is completed afterwards by k_tile_fix)
     T P = Op::ident();
-    if (tile > 0 && !first_head) P = lookback_prefix<Op>(a.lb.word, tile, a.status, a.spin_limit);
+    bool first_head = true;
+    if constexpr (MODE != M_REDUCE) {
+      if (SEG) first_head = (__ldg(a.sv.bits + (base >> 5)) >> (base & 31)) & 1u;
+      else first_head = base == 0;
+      if (tile > 0 && !first_head) P = lookback_prefix<Op>(a.lb.word, tile, a.status, a.spin_limit);
+    }
     if (lane == 0) s_prefix = P;
     named_sync(1, TB_LB);  // carry ready / tile aggregate ready
-    if (lane == 0 && tile > 0 && !first_head && !s_af)
+    if (MODE != M_REDUCE && lane == 0 && tile > 0 && !first_head && !s_af)
       lb_publish(a.lb.word + tile, TS_INC, to_bits<T>(Op::apply(P, s_av)));
     return;
   }
@@ -528,6 +533,7 @@ __global__ void __launch_bounds__(TB_LB, MODE == M_REDUCE ? 7 : 5) k_scan_tma(co
           if (k0 + i + 1 == end) {
             double pv2 = fx_range<ITEMS>(x, ps, i + 1);
             a.out[s] = ((heads >> ps) & 1u) ? pv2 : AddD::apply(run, pv2);
+            if (!pf && !(heads & ((2u << i) - 1u))) a.lead[tile] = s;  // began in an earlier tile
             int s2 = s + 1;
             while (s2 < m && off(s2 + 1) == end) { a.out[s2] = 0.0; ++s2; }
             s = s2;
@@ -543,6 +549,7 @@ __global__ void __launch_bounds__(TB_LB, MODE == M_REDUCE ? 7 : 5) k_scan_tma(co
             run = Op::apply(run, x[i]);
             if (k0 + i + 1 == end) {
               a.out[s] = run;
+              if (!pf && !(heads & ((2u << i) - 1u))) a.lead[tile] = s;  // began in an earlier tile
               int s2 = s + 1;
               while (s2 < m && off(s2 + 1) == end) { a.out[s2] = Op::init(); ++s2; }
               s = s2;
@@ -552,6 +559,66 @@ __global__ void __launch_bounds__(TB_LB, MODE == M_REDUCE ? 7 : 5) k_scan_tma(co
         }
       }
     }
+  }
+}
+
+// Second pass of a segmented reduction: the carry into every tile is the
+// segmented exclusive scan of the tile aggregates (status TS_INC marks a
+// tile holding a segment start; its value is the fold from its last start);
+// the one result per tile whose segment began in an earlier tile gets that
+// carry folded in front.  One CTA: tiles are n / 2048 at most.
+template <class Op>
+__global__ void __launch_bounds__(1024) k_tile_fix(const ulonglong2 *__restrict__ w, const int *__restrict__ lead,
+                                                   int tiles, typename Op::T *out) {
+  typedef typename Op::T T;
+  __shared__ int s_f[32];
+  __shared__ T s_v[32];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int per = (tiles + 1023) / 1024;
+  const int t0 = min(tiles, tid * per), t1 = min(tiles, t0 + per);
+  int f = 0;
+  T v = Op::ident();
+  for (int t = t0; t < t1; t++) {
+    const ulonglong2 q = w[t];
+    const T val = from_bits<T>(q.y);
+    if (q.x == TS_INC) { v = val; f = 1; } else v = Op::apply(v, val);
+  }
+  // exclusive scan of the (flag, value) pairs over the threads
+  int sf = f;
+  T sv = v;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const int f2 = shfl_up(sf, d);
+    const T v2 = shfl_up(sv, d);
+    if (lane >= d) { sv = sf ? sv : Op::apply(v2, sv); sf |= f2; }
+  }
+  if (lane == 31) { s_f[warp] = sf; s_v[warp] = sv; }
+  __syncthreads();
+  if (warp == 0) {
+    int wf = s_f[lane];
+    T wv = s_v[lane];
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const int f2 = shfl_up(wf, d);
+      const T v2 = shfl_up(wv, d);
+      if (lane >= d) { wv = wf ? wv : Op::apply(v2, wv); wf |= f2; }
+    }
+    s_f[lane] = wf;
+    s_v[lane] = wv;
+  }
+  __syncthreads();
+  // carry entering this thread's first tile
+  int ef = shfl_up(sf, 1);
+  T ev = shfl_up(sv, 1);
+  if (lane == 0) { ef = 0; ev = Op::ident(); }
+  T c = ev;
+  if (warp > 0 && !ef) c = Op::apply(s_v[warp - 1], ev);
+  for (int t = t0; t < t1; t++) {
+    const int s = lead[t];
+    if (s >= 0) out[s] = Op::apply(c, out[s]);
+    const ulonglong2 q = w[t];
+    const T val = from_bits<T>(q.y);
+    c = (q.x == TS_INC) ? val : Op::apply(c, val);
   }
 }
 
@@ -591,6 +658,9 @@ template <class T> bool tma_map(CUtensorMap *map, const void *ptr, long rows) {
       CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS;
 }
+// scratch of a TMA-path launch: the look-back area, then (reductions) one
+// int per tile naming the result that k_tile_fix completes
+inline size_t reduce_pass_bytes(int tiles) { return lookback_bytes(tiles) + align_up((size_t)tiles * 4, 256); }
 template <class T> constexpr size_t tma_smem() { return 1024 + (size_t)TT * row_items<T>() * sizeof(T) + WMAX * 4; }
 
 // Returns false (nothing launched) when the vectors do not suit TMA.
@@ -607,7 +677,7 @@ bool run_scan_tma(typename Op::T *out, const typename Op::T *in, vec_p sd, int n
   else tout = tin;
   State &S = st();
   const int tiles = ceil_div(n, (long)TT * row_items<T>());
-  void *mem = scratch_or_work(scratch, lookback_bytes(tiles));
+  void *mem = scratch_or_work(scratch, reduce_pass_bytes(tiles));
   if (!mem) return true;
   TArgs<T> a;
   a.out = out; a.in = in; a.n = n; a.rows = rows;
@@ -615,9 +685,15 @@ bool run_scan_tma(typename Op::T *out, const typename Op::T *in, vec_p sd, int n
   a.lb = lookback_carve(mem, tiles);
   a.status = S.d_status;
   a.spin_limit = S.spin_limit;
+  a.lead = (int *)((char *)a.lb.word + align_up((size_t)tiles * 16, 256));
   GCVL_CK(cudaMemsetAsync(mem, 0, lookback_clear_bytes(tiles), S.stream));
+  if (MODE == M_REDUCE) GCVL_CK(cudaMemsetAsync(a.lead, 0xFF, (size_t)tiles * 4, S.stream));
   k_scan_tma<Op, MODE, SEG><<<tiles, TB_LB, tma_smem<T>(), S.stream>>>(tin, tout, a);
   launch_check(name);
+  if (MODE == M_REDUCE && tiles > 1) {
+    k_tile_fix<Op><<<1, 1024, 0, S.stream>>>(a.lb.word, a.lead, tiles, out);
+    launch_check("k_tile_fix");
+  }
   return true;
 }
 
@@ -770,6 +846,13 @@ void run_reduce(const typename Op::T *in, int n, typename Op::T *result_dev, vec
   k_reduce<Op><<<grid, RBLOCK, 0, S.stream>>>(in, n, partial, ticket, result_dev, count_flags ? 1 : 0);
   launch_check("k_reduce");
 }
+// segmented reductions: the TMA path's look-back area and per-tile
+// fix-up list, or the generic kernel's look-back area
+template <class T> int seg_reduce_units(int n) {
+  if (n <= 0) return 0;
+  const int tiles = ceil_div(n, tile_elems<T>());
+  return (int)((reduce_pass_bytes(tiles) + 7) / 8);
+}
 template <class T> int reduce_units(int n) {
   (void)n;
   return (256 + (st().sm_count > 0 ? st().sm_count : 152) * 2 * 8 + 7) / 8 + 64;
@@ -894,7 +977,7 @@ using namespace gcvl;
     seg_reduce<OP>(d, s, sd, n, m, scratch, false, #NAME "_re" #L);                          \
   }                                                                                          \
   GCVL_EXPORT int NAME##_re##L##_scratch(int n, int m) {                                     \
-    (void)m; int a = scan_units<T>(n), b = reduce_units<T>(n); return a > b ? a : b;         \
+    (void)m; int a = seg_reduce_units<T>(n), b = reduce_units<T>(n); return a > b ? a : b;    \
   }                                                                                          \
   GCVL_EXPORT unsigned NAME##_re##L##_inplace(void) { return INPLACE_NONE; }
 
@@ -938,7 +1021,7 @@ GCVL_EXPORT void pk1_lev(vec_p ds, vec_p f, vec_p sd, int n, int m, vec_p scratc
   seg_reduce<CountB>(ds, f, sd, n, m, scratch, true, "pk1_lev");
 }
 GCVL_EXPORT int pk1_lev_scratch(int n, int m) {
-  (void)m; int a = scan_units<int>(n), b = reduce_units<int>(n); return a > b ? a : b;
+  (void)m; int a = seg_reduce_units<int>(n), b = reduce_units<int>(n); return a > b ? a : b;
 }
 GCVL_EXPORT unsigned pk1_lev_inplace(void) { return INPLACE_NONE; }
 
