@@ -322,6 +322,26 @@ template <int ITEMS> struct Engine<AddD, ITEMS> {
   }
 };
 
+// Reductions: a thread's float64 + fold split between the integer pipes
+// (first half of its items, fixed point) and the FP64 pipe (second half, an
+// add chain), so that neither carries the whole fold.  The segmented
+// reduction has no per-element output work to keep the FP64 pipe busy.
+template <int ITEMS>
+__device__ __forceinline__ void agg_add_split(const double (&x)[ITEMS], unsigned heads, int cnt, int &tf,
+                                              double &tv) {
+  constexpr int H = ITEMS / 2;
+  tf = heads != 0;
+  tv = AddD::ident();
+  if (cnt <= 0) return;
+  const int from = heads ? 31 - __clz((int)heads) : 0;
+  const double lo = fx_range_part<ITEMS, 0, H>(x, from, cnt);
+  double hi = -0.0;
+#pragma unroll
+  for (int i = H; i < ITEMS; i++)
+    if (i >= from && i < cnt) hi = __dadd_rn(hi, x[i]);
+  tv = __dadd_rn(lo, hi);
+}
+
 // The CTA has TT compute threads (one 128-byte row each) plus one look-back
 // warp.  The look-back warp issues the tile's TMA load and at once starts
 // collecting the carry from earlier tiles, while the compute warps fold their
@@ -444,7 +464,8 @@ __global__ void __launch_bounds__(TB_LB, MODE == M_REDUCE ? (sizeof(typename Op:
 
   int tf;
   T tv;
-  Engine<Op, ITEMS>::agg(x, heads, cnt, tf, tv);
+  if constexpr (MODE == M_REDUCE && std::is_same<Op, AddD>::value) agg_add_split<ITEMS>(x, heads, cnt, tf, tv);
+  else Engine<Op, ITEMS>::agg(x, heads, cnt, tf, tv);
 
   // warp inclusive scan of (head, value)
   int f = tf;
@@ -566,60 +587,75 @@ __global__ void __launch_bounds__(TB_LB, MODE == M_REDUCE ? (sizeof(typename Op:
 // segmented exclusive scan of the tile aggregates (status TS_INC marks a
 // tile holding a segment start; its value is the fold from its last start);
 // the one result per tile whose segment began in an earlier tile gets that
-// carry folded in front.  One CTA: tiles are n / 2048 at most.
+// carry folded in front.  One thread per tile, chunks of FIX_NT tiles per
+// CTA joined by a decoupled look-back over the chunks.
+constexpr int FIX_NT = 1024;
 template <class Op>
-__global__ void __launch_bounds__(1024) k_tile_fix(const ulonglong2 *__restrict__ w, const int *__restrict__ lead,
-                                                   int tiles, typename Op::T *out) {
+__global__ void __launch_bounds__(FIX_NT) k_tile_fix(const ulonglong2 *__restrict__ w, const int *__restrict__ lead,
+                                                     int tiles, typename Op::T *out, ulonglong2 *cw,
+                                                     unsigned *status, int spin_limit) {
   typedef typename Op::T T;
-  __shared__ int s_f[32];
-  __shared__ T s_v[32];
+  constexpr int NW = FIX_NT / 32;
+  __shared__ int s_wf[NW];
+  __shared__ T s_wv[NW];
+  __shared__ int s_fa;
+  __shared__ T s_va, s_P;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int per = (tiles + 1023) / 1024;
-  const int t0 = min(tiles, tid * per), t1 = min(tiles, t0 + per);
-  int f = 0;
-  T v = Op::ident();
-  for (int t = t0; t < t1; t++) {
+  const int chunk = blockIdx.x;
+  const int t = chunk * FIX_NT + tid;
+  int fi = 0;
+  T vi = Op::ident();
+  if (t < tiles) {
     const ulonglong2 q = w[t];
-    const T val = from_bits<T>(q.y);
-    if (q.x == TS_INC) { v = val; f = 1; } else v = Op::apply(v, val);
+    fi = q.x == TS_INC;
+    vi = from_bits<T>(q.y);
   }
-  // exclusive scan of the (flag, value) pairs over the threads
-  int sf = f;
-  T sv = v;
 #pragma unroll
   for (int d = 1; d < 32; d <<= 1) {
-    const int f2 = shfl_up(sf, d);
-    const T v2 = shfl_up(sv, d);
-    if (lane >= d) { sv = sf ? sv : Op::apply(v2, sv); sf |= f2; }
+    const int f2 = shfl_up(fi, d);
+    const T v2 = shfl_up(vi, d);
+    if (lane >= d) { vi = fi ? vi : Op::apply(v2, vi); fi |= f2; }
   }
-  if (lane == 31) { s_f[warp] = sf; s_v[warp] = sv; }
+  int ef = shfl_up(fi, 1);
+  T ev = shfl_up(vi, 1);
+  if (lane == 0) { ef = 0; ev = Op::ident(); }
+  if (lane == 31) { s_wf[warp] = fi; s_wv[warp] = vi; }
   __syncthreads();
   if (warp == 0) {
-    int wf = s_f[lane];
-    T wv = s_v[lane];
+    int wf = s_wf[lane];
+    T wv = s_wv[lane];
 #pragma unroll
     for (int d = 1; d < 32; d <<= 1) {
       const int f2 = shfl_up(wf, d);
       const T v2 = shfl_up(wv, d);
       if (lane >= d) { wv = wf ? wv : Op::apply(v2, wv); wf |= f2; }
     }
-    s_f[lane] = wf;
-    s_v[lane] = wv;
+    int xf = shfl_up(wf, 1);
+    T xv = shfl_up(wv, 1);
+    if (lane == 0) { xf = 0; xv = Op::ident(); }
+    const int fa = shfl_idx(wf, NW - 1);
+    const T va = shfl_idx(wv, NW - 1);
+    s_wf[lane] = xf;  // now: exclusive prefix of the warps before
+    s_wv[lane] = xv;
+    if (lane == 0) lb_publish(cw + chunk, (chunk == 0 || fa) ? TS_INC : TS_AGG, to_bits<T>(va));
+    T P = Op::ident();
+    if (chunk > 0) {  // tiles before the chunk's first segment start need the carry
+      P = lookback_prefix<Op>(cw, chunk, status, spin_limit);
+      if (lane == 0 && !fa) lb_publish(cw + chunk, TS_INC, to_bits<T>(Op::apply(P, va)));
+    }
+    if (lane == 0) { s_fa = fa; s_va = va; s_P = P; }
   }
   __syncthreads();
-  // carry entering this thread's first tile
-  int ef = shfl_up(sf, 1);
-  T ev = shfl_up(sv, 1);
-  if (lane == 0) { ef = 0; ev = Op::ident(); }
-  T c = ev;
-  if (warp > 0 && !ef) c = Op::apply(s_v[warp - 1], ev);
-  for (int t = t0; t < t1; t++) {
-    const int s = lead[t];
-    if (s >= 0) out[s] = Op::apply(c, out[s]);
-    const ulonglong2 q = w[t];
-    const T val = from_bits<T>(q.y);
-    c = (q.x == TS_INC) ? val : Op::apply(c, val);
-  }
+  if (t >= tiles) return;
+  const int s = lead[t];
+  if (s < 0) return;
+  // exclusive (flag, value) of this tile within the chunk, then the chunk carry
+  const int pf = s_wf[warp];
+  const T pv = s_wv[warp];
+  const int fe = ef | pf;
+  const T ve = ef ? ev : Op::apply(pv, ev);
+  const T carry = fe ? ve : Op::apply(s_P, ve);
+  out[s] = Op::apply(carry, out[s]);
 }
 
 // Host side: tensor maps and launch.  The driver's tensor-map encoder is
@@ -660,7 +696,10 @@ template <class T> bool tma_map(CUtensorMap *map, const void *ptr, long rows) {
 }
 // scratch of a TMA-path launch: the look-back area, then (reductions) one
 // int per tile naming the result that k_tile_fix completes
-inline size_t reduce_pass_bytes(int tiles) { return lookback_bytes(tiles) + align_up((size_t)tiles * 4, 256); }
+inline size_t reduce_pass_bytes(int tiles) {
+  const int chunks = (tiles + 1023) / 1024;
+  return lookback_bytes(tiles) + align_up((size_t)tiles * 4, 256) + lookback_bytes(chunks);
+}
 template <class T> constexpr size_t tma_smem() { return 1024 + (size_t)TT * row_items<T>() * sizeof(T) + WMAX * 4; }
 
 // Returns false (nothing launched) when the vectors do not suit TMA.
@@ -691,7 +730,11 @@ bool run_scan_tma(typename Op::T *out, const typename Op::T *in, vec_p sd, int n
   k_scan_tma<Op, MODE, SEG><<<tiles, TB_LB, tma_smem<T>(), S.stream>>>(tin, tout, a);
   launch_check(name);
   if (MODE == M_REDUCE && tiles > 1) {
-    k_tile_fix<Op><<<1, 1024, 0, S.stream>>>(a.lb.word, a.lead, tiles, out);
+    const int chunks = ceil_div(tiles, FIX_NT);
+    LookbackMem cl = lookback_carve((char *)a.lead + align_up((size_t)tiles * 4, 256), chunks);
+    GCVL_CK(cudaMemsetAsync(cl.counter, 0, 256 + (size_t)chunks * 16, S.stream));
+    k_tile_fix<Op><<<chunks, FIX_NT, 0, S.stream>>>(a.lb.word, a.lead, tiles, out, cl.word, S.d_status,
+                                                   S.spin_limit);
     launch_check("k_tile_fix");
   }
   return true;

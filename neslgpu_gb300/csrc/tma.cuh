@@ -110,6 +110,27 @@ __device__ __forceinline__ double fx_to_double(long long acc, int emax) {
   return scalbn(v, emax - 1075);
 }
 
+// The fixed-point sum of the items of x[LO..HI) that lie in [from, to).
+template <int ITEMS, int LO, int HI>
+__device__ __forceinline__ double fx_range_part(const double (&x)[ITEMS], int from, int to) {
+  int emax = 1;
+#pragma unroll
+  for (int i = LO; i < HI; i++)
+    if (i >= from && i < to) emax = max(emax, fx_exp((unsigned long long)__double_as_longlong(x[i])));
+  if (emax == 2047) {
+    double v = -0.0;
+#pragma unroll
+    for (int i = LO; i < HI; i++)
+      if (i >= from && i < to) v = __dadd_rn(v, x[i]);
+    return v;
+  }
+  long long acc = 0;
+#pragma unroll
+  for (int i = LO; i < HI; i++)
+    if (i >= from && i < to) fx_add(acc, (unsigned long long)__double_as_longlong(x[i]), emax);
+  return fx_to_double(acc, emax);
+}
+
 // Sum of x[from..to) by the fixed-point path (FP64 when inf/NaN present).
 template <int ITEMS>
 __device__ __forceinline__ double fx_range(const double (&x)[ITEMS], int from, int to) {

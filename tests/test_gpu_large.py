@@ -56,3 +56,25 @@ def test_default_permute_wider_destination(gpu, oracle, data):
     dflt = np.full(nd, -7, dtype=np.int32)
     compare("exact", ops.dpe_u(gpu, "dpe_puz", data["xi"], idx, dflt),
             ops.dpe_u(oracle, "dpe_puz", data["xi"], idx, dflt))
+
+
+@pytest.mark.parametrize("kind", ["lognormal", "few_long"])
+def test_segmented_reductions_many_chunks(gpu, oracle, kind):
+    """Reductions over more than 1024 tiles with segments that span tiles
+    and chunks of tiles: the second pass's chunked look-back."""
+    from cases import seg_abs_total
+    r = W.rng(77)
+    n = (1 << 22) + 77
+    if kind == "lognormal":
+        lens = W.lognormal_lengths(r, n, 5.0, 2.0, 1 << 20)
+    else:
+        lens = np.array([1 << 21, 5, (1 << 21) - 5, 77], dtype=np.int32)
+    lens = W.with_empty(r, lens, 0.05)
+    xd = W.float64_normal(r, n)
+    xi = r.integers(-1000, 1000, size=n).astype(np.int32)
+    fl = (r.random(n) < 0.5).astype(np.int32)
+    got = ops.reduce_e(gpu, "add_red", xd, lens)
+    compare("sum", got, ops.reduce_e(oracle, "add_red", xd, lens), seg_abs_total(xd, lens))
+    for name, x in (("add_rez", xi), ("max_rez", xi), ("min_red", xd)):
+        compare("exact", ops.reduce_e(gpu, name, x, lens), ops.reduce_e(oracle, name, x, lens))
+    compare("exact", ops.pk1_e(gpu, fl, lens), ops.pk1_e(oracle, fl, lens))
