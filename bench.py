@@ -291,12 +291,13 @@ def dispatch_suite(g, count=512, hi=24, seed=2024):
     return out
 
 
-def _vcode_sort(cvl, keys, sync):
+def _vcode_sort(cvl, keys, sync, fused=None):
     """QSORT through the VCODE interpreter: (seconds with the keys on the
     device, seconds end to end from host keys to host result, sorted keys,
-    VCODE ops run)."""
+    VCODE ops run).  fused: a FusedLib, to run the .fcode form instead."""
     from neslgpu_gb300 import vcode as V, vcode_programs as P
-    it = V.Interpreter(P.qsort_program(), cvl, sync=sync)
+    text = P.qsort_fcode_program()[0] if fused is not None else P.qsort_program()
+    it = V.Interpreter(text, cvl, sync=sync, fused=fused)
     try:
         t0 = time.perf_counter()
         lv = it.from_host("I", [len(keys)])
@@ -333,6 +334,13 @@ def vinterp_suite(g, log2n=26, log2rows=22, seed=2026, cpu_sample_log2n=20):
     qs = {"n": n, "keys": "uniform int32, seeded", "seconds": round(dev_s, 4),
           "mkeys_s": round(n / dev_s / 1e6, 2), "e2e_seconds": round(e2e_s, 4),
           "e2e_mkeys_s": round(n / e2e_s / 1e6, 2), "vcode_ops": ops, "sorted": ok}
+    # the .fcode form: elementwise chains as generated fused kernels
+    from neslgpu_gb300 import fcode as F, vcode_programs as P
+    lib = F.FusedLib(P.qsort_fcode_program()[1])
+    _vcode_sort(c, keys[: 1 << 16], sync, lib)
+    fdev, fe2e, fout, fops = _vcode_sort(c, keys, sync, lib)
+    qs["fcode"] = {"seconds": round(fdev, 4), "mkeys_s": round(n / fdev / 1e6, 2), "vcode_ops": fops,
+                   "same_result": bool(np.array_equal(fout, out)), "speedup_vs_vcode": round(dev_s / fdev, 3)}
     if cpu_sample_log2n:
         # the same interpreter and program on the oracle's serial CVL
         # restatement, one host thread, on a bounded sample

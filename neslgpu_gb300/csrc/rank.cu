@@ -30,11 +30,15 @@
 // window scatter for large vectors.
 #include "gcvl.cuh"
 
+#include <type_traits>
 #include <utility>
 
 namespace gcvl {
 
-constexpr int RK_BLOCK = 256, RK_ITEMS = 16, RK_TILE = RK_BLOCK * RK_ITEMS;
+#ifndef GCVL_RK_ITEMS
+#define GCVL_RK_ITEMS 16
+#endif
+constexpr int RK_BLOCK = 256, RK_ITEMS = GCVL_RK_ITEMS, RK_TILE = RK_BLOCK * RK_ITEMS;
 constexpr int RK_WARPS = RK_BLOCK / 32;
 constexpr int RK_MAXPASS = 12;
 constexpr int RK_LB = 32;  // predecessors read per look-back round trip
@@ -164,13 +168,17 @@ template <class K, class V> struct PassArgs {
   int spin_limit;
 };
 
-template <class K, class V, bool AUX> constexpr size_t pass_smem() {
+template <class K, class V, bool AUX, bool STABLE = true> constexpr size_t pass_smem() {
   return (size_t)RK_TILE * (2 * sizeof(K) + 2 * sizeof(V) + (AUX ? 8 : 0)) + RK_WARPS * 256 * 2 + 256 * 4 +
          256 * 8;
 }
 
-template <class K, class V, bool AUX, int IN, int OUT>
+// STABLE: equal digits keep their order (every pass of a rank).  A pass
+// that only groups pairs by output window (the partitioned scatter) need
+// not: its slots come from shared-memory atomics instead of ballots.
+template <class K, class V, bool AUX, int IN, int OUT, bool STABLE = true>
 __global__ void __launch_bounds__(RK_BLOCK, 2) k_radix_pass(PassArgs<K, V> a) {
+  typedef unsigned short CntT;  // per-warp digit counts (at most 512)
   extern __shared__ __align__(16) unsigned char rk_smem[];
   // staged tile (input order) and the reordered tile
   long long *s_gb = (long long *)rk_smem;                  // [256] global base per digit
@@ -181,7 +189,7 @@ __global__ void __launch_bounds__(RK_BLOCK, 2) k_radix_pass(PassArgs<K, V> a) {
   unsigned *s_ain = (unsigned *)(s_vout + RK_TILE);
   unsigned *s_aout = s_ain + (AUX ? RK_TILE : 0);
   unsigned *s_loc = s_aout + (AUX ? RK_TILE : 0);          // [256] tile offset per digit
-  unsigned short *s_cnt = (unsigned short *)(s_loc + 256);  // [RK_WARPS][256]
+  CntT *s_cnt = (CntT *)(s_loc + 256);                      // [RK_WARPS][256]
   __shared__ unsigned s_tile;
   __shared__ unsigned s_ws[RK_WARPS];
 
@@ -213,21 +221,30 @@ __global__ void __launch_bounds__(RK_BLOCK, 2) k_radix_pass(PassArgs<K, V> a) {
   }
   __syncthreads();
 
-  // stable rank within each warp's 512 elements: (rank << 8) | digit
+  // rank within each warp's 512 elements: (rank << 8) | digit
   const int wbase = warp * 32 * RK_ITEMS;
-  unsigned short *cnt = s_cnt + warp * 256;
+  CntT *cnt = s_cnt + warp * 256;
   const unsigned lt = (1u << lane) - 1u;
   unsigned wr[RK_ITEMS];
 #pragma unroll
   for (int c = 0; c < RK_ITEMS; c++) {
     const int e = wbase + c * 32 + lane;
     const int d = e < valid ? (int)((s_kin[e] >> a.shift) & 255) : -1;
-    const unsigned peers = warp_match8(d);
     unsigned r = 0;
-    if (d >= 0) r = cnt[d] + __popc(peers & lt);
-    __syncwarp();
-    if (d >= 0 && (peers & lt) == 0) cnt[d] = (unsigned short)(cnt[d] + __popc(peers));
-    __syncwarp();
+    if constexpr (STABLE) {
+      const unsigned peers = warp_match8(d);
+      if (d >= 0) r = cnt[d] + __popc(peers & lt);
+      __syncwarp();
+      if (d >= 0 && (peers & lt) == 0) cnt[d] = (CntT)(cnt[d] + __popc(peers));
+      __syncwarp();
+    } else {
+      // a slot from a shared-memory atomic on the 32-bit word holding the
+      // digit's 16-bit count
+      if (d >= 0) {
+        const unsigned sh = (d & 1) * 16;
+        r = (atomicAdd((unsigned *)(cnt + (d & ~1)), 1u << sh) >> sh) & 0xFFFFu;
+      }
+    }
     wr[c] = d >= 0 ? (r << 8) | (unsigned)d : 0xFFFFFFFFu;
   }
   __syncthreads();
@@ -238,7 +255,7 @@ __global__ void __launch_bounds__(RK_BLOCK, 2) k_radix_pass(PassArgs<K, V> a) {
 #pragma unroll
   for (int w = 0; w < RK_WARPS; w++) {
     unsigned c = s_cnt[w * 256 + dd];
-    s_cnt[w * 256 + dd] = (unsigned short)tot;
+    s_cnt[w * 256 + dd] = (CntT)tot;
     tot += c;
   }
   // publish this tile's digit count, then look back for earlier tiles'.
@@ -358,16 +375,16 @@ __global__ void __launch_bounds__(RK_BLOCK) k_window_scatter(V *__restrict__ d, 
   }
 }
 
-template <class K, class V, bool AUX, int IN, int OUT>
+template <class K, class V, bool AUX, int IN, int OUT, bool STABLE = true>
 void launch_pass(const PassArgs<K, V> &a, int tiles) {
-  constexpr size_t sm = pass_smem<K, V, AUX>();
+  constexpr size_t sm = pass_smem<K, V, AUX, STABLE>();
   static bool attr = false;
   if (!attr) {
-    GCVL_CK(cudaFuncSetAttribute(k_radix_pass<K, V, AUX, IN, OUT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)sm));
+    GCVL_CK(cudaFuncSetAttribute(k_radix_pass<K, V, AUX, IN, OUT, STABLE>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     attr = true;
   }
-  k_radix_pass<K, V, AUX, IN, OUT><<<tiles, RK_BLOCK, sm, stream()>>>(a);
+  k_radix_pass<K, V, AUX, IN, OUT, STABLE><<<tiles, RK_BLOCK, sm, stream()>>>(a);
   launch_check("k_radix_pass");
 }
 
@@ -422,7 +439,7 @@ void scatter_partitioned(V *d, const V *s, const int *idx, int n, int n_d, vec_p
   a.kout = (unsigned *)(mem + L.kout); a.vout = (V *)(mem + L.vout);
   a.starts = hist; a.state = state; a.counter = counter;
   a.n = n; a.shift = shift; a.status = S.d_status; a.spin_limit = S.spin_limit;
-  launch_pass<unsigned, V, false, IN_ARRAYS, OUT_ARRAYS>(a, tiles);
+  launch_pass<unsigned, V, false, IN_ARRAYS, OUT_ARRAYS, false>(a, tiles);
   const long g = ((long)n + RK_BLOCK * SC_ITEMS - 1) / (RK_BLOCK * SC_ITEMS);
   k_window_scatter<V><<<(int)g, RK_BLOCK, 0, S.stream>>>(d, a.kout, a.vout, n);
   launch_check("k_window_scatter");
@@ -559,7 +576,7 @@ void rank_impl(vec_p d, vec_p s, vec_p sd, int n, int m, vec_p scratch, int is_d
     a.kout = iA; a.vout = (unsigned *)kA;  // free: the last pass read (kA, iA)
     a.starts = wst; a.state = state; a.counter = counters + RK_MAXPASS;
     a.n = n; a.shift = shift; a.status = S.d_status; a.spin_limit = S.spin_limit;
-    launch_pass<unsigned, unsigned, false, IN_ARRAYS, OUT_ARRAYS>(a, tiles);
+    launch_pass<unsigned, unsigned, false, IN_ARRAYS, OUT_ARRAYS, false>(a, tiles);
     const long g = ((long)n + RK_BLOCK * SC_ITEMS - 1) / (RK_BLOCK * SC_ITEMS);
     k_window_scatter<unsigned><<<(int)g, RK_BLOCK, 0, S.stream>>>((unsigned *)d, iA, (const unsigned *)kA, n);
     launch_check("k_window_scatter");

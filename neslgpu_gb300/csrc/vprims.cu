@@ -41,6 +41,98 @@ template <class F> void segwalk(F f, const SegView &sv, const char *name) {
   k_segwalk<F><<<grid_for(((long)sv.n + SITEMS - 1) / SITEMS, VBLOCK), VBLOCK, 0, stream()>>>(f, sv);
   launch_check(name);
 }
+// Segmented maps whose result is one value per element (DIST, INDEX,
+// segmented BPERMUTE): a warp owns SMI*32 consecutive elements, each lane
+// SMI consecutive ones.  Phase 1 walks the lane's elements through the
+// segment descriptor (one segment lookup, then a walk) and records a token
+// per element (the segment, or the source address); phase 2 fetches all
+// the lane's values at once (independent loads in flight); the values pass
+// through shared memory so that every global load and store is coalesced.
+constexpr int SMI = 16, SMB = 128;
+template <class F>
+__global__ void __launch_bounds__(SMB) k_segmap(F f, SegView sv) {
+  typedef typename F::T T;
+  constexpr int WE = 32 * SMI, PADW = WE + 32;
+  __shared__ T s_val[SMB / 32][PADW];
+  __shared__ int s_aux[F::AUX ? SMB / 32 : 1][F::AUX ? PADW : 1];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const long wbase = ((long)blockIdx.x * (SMB / 32) + warp) * WE;
+  if (wbase >= sv.n) return;
+  const int wcnt = (int)min((long)WE, (long)sv.n - wbase);
+  if constexpr (F::AUX) {
+#pragma unroll
+    for (int j = 0; j < SMI; j++) {
+      const int e = j * 32 + lane;
+      if (e < wcnt) s_aux[warp][e + e / SMI] = __ldcs(f.aux + wbase + e);
+    }
+    __syncwarp();
+  }
+  const int e0 = lane * SMI;
+  const int cnt = max(0, min(SMI, wcnt - e0));
+  long long tok[SMI];
+  if (cnt > 0) {
+    const int k0 = (int)(wbase + e0);
+    int sg = seg_of(sv, k0);
+    int start = __ldg(sv.off + sg), end = __ldg(sv.off + sg + 1);
+#pragma unroll
+    for (int i = 0; i < SMI; i++) {
+      if (i < cnt) {
+        const int k = k0 + i;
+        while (k >= end) { ++sg; start = end; end = __ldg(sv.off + sg + 1); }
+        int a = 0;
+        if constexpr (F::AUX) a = s_aux[warp][e0 + lane + i];
+        tok[i] = f.token(k, sg, start, a);
+        // values that come from a per-segment table are fetched in the walk
+        if constexpr (!F::GATHER) s_val[warp][e0 + lane + i] = f.fetch(tok[i]);
+      }
+    }
+  }
+  if constexpr (F::GATHER) {  // all of the lane's gathers in flight at once
+    T v[SMI];
+#pragma unroll
+    for (int i = 0; i < SMI; i++)
+      if (i < cnt) v[i] = f.fetch(tok[i]);
+#pragma unroll
+    for (int i = 0; i < SMI; i++)
+      if (i < cnt) s_val[warp][e0 + lane + i] = v[i];
+  }
+  __syncwarp();
+#pragma unroll
+  for (int j = 0; j < SMI; j++) {
+    const int e = j * 32 + lane;
+    if (e < wcnt) __stcs(f.d + wbase + e, s_val[warp][e + e / SMI]);
+  }
+}
+template <class F> void segmap(F f, const SegView &sv, const char *name) {
+  if (sv.n <= 0 || sv.m <= 0) return;
+  const long per = (long)SMB * SMI;
+  k_segmap<F><<<(int)((sv.n + per - 1) / per), SMB, 0, stream()>>>(f, sv);
+  launch_check(name);
+}
+template <class TT> struct DisMap {  // d[k] = v[seg(k)]
+  typedef TT T;
+  static constexpr bool AUX = false, GATHER = false;
+  T *d; const T *v; const int *aux;
+  __device__ long long token(int, int s, int, int) const { return s; }
+  __device__ T fetch(long long s) const { return __ldg(v + s); }
+};
+struct IndMap {  // d[k] = init[s] + stride[s] * (k - start)
+  typedef int T;
+  static constexpr bool AUX = false, GATHER = false;
+  int *d; const int *init; const int *stride; const int *aux;
+  __device__ long long token(int k, int s, int start, int) const {
+    return (int)((unsigned)__ldg(init + s) + (unsigned)__ldg(stride + s) * (unsigned)(k - start));
+  }
+  __device__ int fetch(long long v) const { return (int)v; }
+};
+template <class TT> struct BPermMap {  // d[k] = s[off_s[seg_d(k)] + i[k]], as many source as dest segments
+  typedef TT T;
+  static constexpr bool AUX = true, GATHER = true;
+  T *d; const T *src; const int *off_s; const int *aux;
+  __device__ long long token(int, int s, int, int i) const { return (long long)__ldg(off_s + s) + i; }
+  __device__ T fetch(long long at) const { return __ldg(src + at); }
+};
+
 // f(i) for i in [0, n)
 template <class F> __global__ void __launch_bounds__(VBLOCK) k_each(F f, long n) {
   const long stride = (long)gridDim.x * VBLOCK;
@@ -338,7 +430,7 @@ using namespace gcvl;
   META_SEG(rep_ve##L, INPLACE_NONE)                                                    \
   GCVL_EXPORT void dis_ve##L(vec_p d, vec_p v, vec_p sd, int n, int m, vec_p scratch) { \
     (void)scratch; ensure_init();                                                     \
-    segwalk(DisSeg<T>{(T *)d, (const T *)v}, seg_view(sd, n, m), "dis_ve" #L);        \
+    segmap(DisMap<T>{(T *)d, (const T *)v, nullptr}, seg_view(sd, n, m), "dis_ve" #L); \
   }                                                                                    \
   META_SEG(dis_ve##L, INPLACE_NONE)
 EXT_REP(z, int)
@@ -369,7 +461,7 @@ META1(rep_vud, INPLACE_NONE)
 // Segmented index (library.c:28-49).
 GCVL_EXPORT void ind_lez(vec_p d, vec_p init, vec_p stride, vec_p sd, int n, int m, vec_p scratch) {
   (void)scratch; ensure_init();
-  segwalk(IndSeg{(int *)d, (const int *)init, (const int *)stride}, seg_view(sd, n, m), "ind_lez");
+  segmap(IndMap{(int *)d, (const int *)init, (const int *)stride, nullptr}, seg_view(sd, n, m), "ind_lez");
 }
 META_SEG(ind_lez, INPLACE_NONE)
 
@@ -400,8 +492,12 @@ META_SEG(ind_lez, INPLACE_NONE)
     (void)scratch; ensure_init();                                                       \
     if (m_s == 1) { gather<T>((T *)d, (const T *)s, (const int *)i, n_d, "bck_pe" #L); return; } \
     SegView ss = seg_view(sd_s, n_s, m_s);                                              \
-    segwalk(BPermSeg<T>{(T *)d, (const T *)s, (const int *)i, ss.off, m_s},                 \
-            seg_view(sd_d, n_d, m_d), "bck_pe" #L);                                     \
+    if (m_s == m_d)                                                                     \
+      segmap(BPermMap<T>{(T *)d, (const T *)s, ss.off, (const int *)i},                  \
+             seg_view(sd_d, n_d, m_d), "bck_pe" #L);                                    \
+    else                                                                                \
+      segwalk(BPermSeg<T>{(T *)d, (const T *)s, (const int *)i, ss.off, m_s},               \
+              seg_view(sd_d, n_d, m_d), "bck_pe" #L);                                   \
   }                                                                                     \
   META_SEG2(bck_pe##L, INPLACE_2)                                                       \
   GCVL_EXPORT void fpm_pu##L(vec_p d, vec_p s, vec_p i, vec_p f, int len_src,           \

@@ -156,6 +156,9 @@ def parse(text: str) -> tuple[list[Ins], dict[str, int], str]:
             else:
                 prog.append(Ins("CONST", typ, toks[i][0], None, ln))
                 i += 1
+        elif t == "FUSED":
+            prog.append(Ins("FUSED", None, int(toks[i][0]), None, ln))
+            i += 1
         elif t in ("START_TIMER", "STOP_TIMER", "EXIT", "MAKE_SEGDES", "LENGTHS", "PAIR", "UNPAIR", "FOPEN",
                    "FCLOSE", "FREAD_CHAR", "SPAWN"):
             prog.append(Ins(t, line=ln))
@@ -233,7 +236,9 @@ class Heap:
 class Interpreter:
     """Runs a parsed VCODE program on one CVL implementation."""
 
-    def __init__(self, text: str, cvl: CVL | None = None, sync=None):
+    def __init__(self, text: str, cvl: CVL | None = None, sync=None, fused=None):
+        """fused: a FusedLib (neslgpu_gb300.fcode) for the program's FUSED ops."""
+        self.fused = fused
         self.c = c = cvl or load()
         self.prog, self.funcs, self.main = parse(text)
         self.heap = Heap(c)
@@ -593,6 +598,18 @@ class Interpreter:
                           sdd.seg_len, sdd.len,
                           self.scratch(self.sfn(name + "_scratch")(sds.seg_len, sds.len, sdd.seg_len, sdd.len)))
             self._finish(6, [d])
+        elif op == "FUSED":
+            fz = self.fused
+            if fz is None:
+                raise VcodeError(f"line {ins.line}: FUSED {ins.a} without a fused library")
+            k = ins.a
+            ar = fz.arity(k)
+            args = st[-ar:]
+            a0 = args[0]
+            L = a0.seg_len if a0.kind == "S" else a0.len
+            d = self.new(fz.result_kind(k), L)
+            fz.fn[k](d.ptr, *[a.ptr for a in args], L, None)
+            self._finish(ar, [d])
         elif op == "SRAND":
             s = st[-1]
             self.fn("rnd_foz")(self.scalar_int(s))

@@ -14,13 +14,16 @@
 * ``SPMV`` -- y = A x for A stored as a nested sequence of (column, value)
   rows (CSR): BPERMUTE gathers x by column, elementwise product, segmented
   +_REDUCE per row.
+* ``qsort_fcode_program`` -- QSORT with its elementwise chains replaced by
+  ``FUSED k`` super-ops, in the form the NESL fusion compiler produces (an
+  .fcode program plus the super-op definitions), for ``neslgpu_gb300.fcode``.
 """
 from __future__ import annotations
 
 from .vcode_asm import Block, Func
 
 
-def _qs_loop() -> str:
+def _qs_loop(fused: bool = False) -> str:
     f = Func("QS_LOOP", params=["keys", "sd"], results=["out"])
     f.op("LENGTHS", ["sd"], ["lens"])
     f.op("MIN_REDUCE INT", ["keys", "sd"], ["mn"])
@@ -35,17 +38,25 @@ def _qs_loop() -> str:
 
     t = Block()
     # pivot: element #a/2 of each segment
-    t.const("INT 2", "two")
-    t.op("DIST INT", ["two", "one_m"], ["twos"])
-    t.op("/ INT", ["lens", "twos"], ["mid"])
+    if fused:
+        t.op("FUSED 0", ["lens", "one_m"], ["mid"])          # lens / 2
+    else:
+        t.const("INT 2", "two")
+        t.op("DIST INT", ["two", "one_m"], ["twos"])
+        t.op("/ INT", ["lens", "twos"], ["mid"])
     t.op("EXTRACT INT", ["keys", "mid", "sd"], ["piv"])
     t.op("DIST INT", ["piv", "sd"], ["pv"])
-    t.op("< INT", ["keys", "pv"], ["lt"])
-    t.op("= INT", ["keys", "pv"], ["eq"])
-    t.op("> INT", ["keys", "pv"], ["gt"])
-    t.op("B_TO_I", ["lt"], ["lti"])
-    t.op("B_TO_I", ["eq"], ["eqi"])
-    t.op("B_TO_I", ["gt"], ["gti"])
+    if fused:
+        t.op("FUSED 1", ["keys", "pv"], ["lti"])             # B_TO_I (keys < pv)
+        t.op("FUSED 2", ["keys", "pv"], ["eqi"])             # B_TO_I (keys = pv)
+        t.op("FUSED 3", ["keys", "pv"], ["gti"])             # B_TO_I (keys > pv)
+    else:
+        t.op("< INT", ["keys", "pv"], ["lt"])
+        t.op("= INT", ["keys", "pv"], ["eq"])
+        t.op("> INT", ["keys", "pv"], ["gt"])
+        t.op("B_TO_I", ["lt"], ["lti"])
+        t.op("B_TO_I", ["eq"], ["eqi"])
+        t.op("B_TO_I", ["gt"], ["gti"])
     t.op("+_REDUCE INT", ["lti", "sd"], ["clt"])
     t.op("+_REDUCE INT", ["eqi", "sd"], ["ceq"])
     t.op("+_REDUCE INT", ["gti", "sd"], ["cgt"])
@@ -53,12 +64,15 @@ def _qs_loop() -> str:
     t.op("+_SCAN INT", ["eqi", "sd"], ["peq0"])
     t.op("+_SCAN INT", ["gti", "sd"], ["pgt0"])
     t.op("DIST INT", ["clt", "sd"], ["dlt"])
-    t.op("+ INT", ["peq0", "dlt"], ["peq"])
     t.op("+ INT", ["clt", "ceq"], ["clteq"])
     t.op("DIST INT", ["clteq", "sd"], ["dlteq"])
-    t.op("+ INT", ["pgt0", "dlteq"], ["pgt"])
-    t.op("SELECT INT", ["eq", "peq", "pgt"], ["pos1"])
-    t.op("SELECT INT", ["lt", "plt", "pos1"], ["pos"])
+    if fused:  # the whole position computation in one pass
+        t.op("FUSED 4", ["lti", "eqi", "plt", "peq0", "dlt", "pgt0", "dlteq"], ["pos"])
+    else:
+        t.op("+ INT", ["peq0", "dlt"], ["peq"])
+        t.op("+ INT", ["pgt0", "dlteq"], ["pgt"])
+        t.op("SELECT INT", ["eq", "peq", "pgt"], ["pos1"])
+        t.op("SELECT INT", ["lt", "plt", "pos1"], ["pos"])
     t.op("PERMUTE INT", ["keys", "pos", "sd"], ["keys2"])
     # next lengths: (lesser, equal, greater) of every segment, interleaved
     t.const("INT 3", "three")
@@ -73,8 +87,11 @@ def _qs_loop() -> str:
     t.op("DPERMUTE INT", ["clt", "i0", "z3", "one_m", "one_3m"], ["l1"])
     t.op("DPERMUTE INT", ["ceq", "i1", "l1", "one_m", "one_3m"], ["l2"])
     t.op("DPERMUTE INT", ["cgt", "i2", "l2", "one_m", "one_3m"], ["l3"])
-    t.op("DIST INT", ["zero", "one_3m"], ["zz"])
-    t.op("> INT", ["l3", "zz"], ["nonempty"])
+    if fused:
+        t.op("FUSED 5", ["l3", "one_3m"], ["nonempty"])    # l3 > 0
+    else:
+        t.op("DIST INT", ["zero", "one_3m"], ["zz"])
+        t.op("> INT", ["l3", "zz"], ["nonempty"])
     t.op("PACK INT", ["l3", "nonempty", "one_3m"], ["l4", "l4sd"])
     t.op("MAKE_SEGDES", ["l4"], ["sd2"])
     t.call("QS_LOOP", ["keys2", "sd2"], ["out"])
@@ -85,12 +102,29 @@ def _qs_loop() -> str:
     return f.emit()
 
 
-def qsort_program() -> str:
+def qsort_program(fused: bool = False) -> str:
     """FUNC QSORT: (sd, keys) -> (sd, sorted keys), sd one segment."""
     main = Func("QSORT", params=["sd", "keys"], results=["sd", "out"])
     main.call("QS_LOOP", ["keys", "sd"], ["out"])
     return "{ quicksort of an int sequence; generated by neslgpu_gb300/vcode_programs.py }\n" + \
-        main.emit() + "\n" + _qs_loop()
+        main.emit() + "\n" + _qs_loop(fused)
+
+
+# the super-ops of qsort_fcode_program, in the fusion compiler's notation
+QSORT_FUSED_DEFS = """
+fused OP0#1 ($0 : INT, $1 : SEGDES) = (/ INT @ $0 (DIST INT @ (CONST INT 2) $1))
+fused OP1#1 ($0 : INT, $1 : INT) = (B_TO_I @ (< INT @ $0 $1))
+fused OP2#1 ($0 : INT, $1 : INT) = (B_TO_I @ (= INT @ $0 $1))
+fused OP3#1 ($0 : INT, $1 : INT) = (B_TO_I @ (> INT @ $0 $1))
+fused OP4#1 ($0 : INT, $1 : INT, $2 : INT, $3 : INT, $4 : INT, $5 : INT, $6 : INT) =
+  (SELECT INT @ (I_TO_B @ $0) $2 (SELECT INT @ (I_TO_B @ $1) (+ INT @ $3 $4) (+ INT @ $5 $6)))
+fused OP5#1 ($0 : INT, $1 : SEGDES) = (> INT @ $0 (DIST INT @ (CONST INT 0) $1))
+"""
+
+
+def qsort_fcode_program() -> tuple[str, str]:
+    """(the .fcode program, its super-op definitions)."""
+    return qsort_program(fused=True), QSORT_FUSED_DEFS
 
 
 def spmv_program() -> str:
