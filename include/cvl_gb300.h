@@ -720,6 +720,12 @@ int gcvl_sync(void);
 /* The library stream (a cudaStream_t); set NULL to restore the library's own. */
 void *gcvl_get_stream(void);
 void gcvl_set_stream(void *stream);
+/* A new non-blocking stream on the library's device (NULL on failure), and
+ * its release.  No counterpart in the reference, whose CVL has one implicit
+ * stream: two streams let transfers of one piece of a vector overlap the
+ * kernels of another. */
+void *gcvl_stream_create(void);
+void gcvl_stream_destroy(void *stream);
 int gcvl_sm_count(void);
 int gcvl_device(void);
 /* Iteration limit of every bounded device wait (failure-detection tests). */

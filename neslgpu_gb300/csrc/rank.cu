@@ -117,16 +117,49 @@ __global__ void __launch_bounds__(RK_BLOCK) k_rank_prep(RankPrep p) {
     if (s_hist[i]) atomicAdd(&p.hist[i], s_hist[i]);
 }
 
-// histogram of one digit of 32-bit keys (the partition of a scatter)
-__global__ void __launch_bounds__(RK_BLOCK) k_digit_hist(const unsigned *key, long n, int shift, unsigned *hist) {
+// histogram of one digit of 32-bit keys (the partition of a scatter); with
+// `unsorted` non-null it also records whether any key exceeds its successor
+__global__ void __launch_bounds__(RK_BLOCK) k_digit_hist(const unsigned *key, long n, int shift, unsigned *hist,
+                                                         unsigned *unsorted) {
   __shared__ unsigned s_hist[256];
+  __shared__ int s_uns;
   s_hist[threadIdx.x] = 0;
+  if (threadIdx.x == 0) s_uns = 0;
   __syncthreads();
   const long stride = (long)gridDim.x * RK_BLOCK;
-  for (long i = (long)blockIdx.x * RK_BLOCK + threadIdx.x; i < n; i += stride)
-    atomicAdd(&s_hist[(__ldcs(key + i) >> shift) & 255], 1u);
+  int uns = 0;
+  for (long i = (long)blockIdx.x * RK_BLOCK + threadIdx.x; i < n; i += stride) {
+    const unsigned k = __ldcs(key + i);
+    atomicAdd(&s_hist[(k >> shift) & 255], 1u);
+    // the successor's load usually hits the line just read by the next lane
+    if (unsorted && i + 1 < n && k > __ldg(key + i + 1)) uns = 1;
+  }
+  if (unsorted && __any_sync(0xffffffffu, uns) && (threadIdx.x & 31) == 0) s_uns = 1;
   __syncthreads();
   if (s_hist[threadIdx.x]) atomicAdd(&hist[threadIdx.x], s_hist[threadIdx.x]);
+  if (threadIdx.x == 0 && s_uns) atomicOr(unsorted, 1u);
+}
+
+// d[idx[i]] = s[i] when the indices ascend (gate word zero): the stores of a
+// warp then fall on few lines, and no partition is needed
+template <class V>
+__global__ void __launch_bounds__(RK_BLOCK) k_sorted_scatter(V *__restrict__ d, const V *__restrict__ s,
+                                                             const int *__restrict__ idx, long n,
+                                                             const unsigned *__restrict__ gate) {
+  if (*(const volatile unsigned *)gate) return;
+  const long i0 = (long)blockIdx.x * (RK_BLOCK * SC_ITEMS) + threadIdx.x;
+  int k[SC_ITEMS];
+  V v[SC_ITEMS];
+#pragma unroll
+  for (int u = 0; u < SC_ITEMS; u++) {
+    const long i = i0 + (long)u * RK_BLOCK;
+    if (i < n) { k[u] = __ldcs(idx + i); v[u] = __ldcs(s + i); }
+  }
+#pragma unroll
+  for (int u = 0; u < SC_ITEMS; u++) {
+    const long i = i0 + (long)u * RK_BLOCK;
+    if (i < n) d[k[u]] = v[u];
+  }
 }
 
 // hist[q][d] -> exclusive scan over d, in place (one CTA, 256 threads)
@@ -163,6 +196,7 @@ template <class K, class V> struct PassArgs {
   const unsigned *starts;             // this pass's digit starts
   unsigned *state;                    // [tiles][256] look-back words
   unsigned *counter;
+  const unsigned *gate;               // non-null: the pass runs only if *gate is non-zero
   int n, shift;
   unsigned *status;
   int spin_limit;
@@ -194,6 +228,7 @@ __global__ void __launch_bounds__(RK_BLOCK, 2) k_radix_pass(PassArgs<K, V> a) {
   __shared__ unsigned s_ws[RK_WARPS];
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (a.gate && *(const volatile unsigned *)a.gate == 0) return;  // the same answer for every CTA
   if (tid == 0) s_tile = atomicAdd(a.counter, 1u);
   for (int i = tid; i < RK_WARPS * 256; i += RK_BLOCK) s_cnt[i] = 0;
   __syncthreads();
@@ -359,7 +394,9 @@ __global__ void __launch_bounds__(RK_BLOCK, 2) k_radix_pass(PassArgs<K, V> a) {
 // output window
 template <class V>
 __global__ void __launch_bounds__(RK_BLOCK) k_window_scatter(V *__restrict__ d, const unsigned *__restrict__ key,
-                                                             const V *__restrict__ val, long n) {
+                                                             const V *__restrict__ val, long n,
+                                                             const unsigned *__restrict__ gate) {
+  if (gate && *(const volatile unsigned *)gate == 0) return;
   const long i0 = (long)blockIdx.x * (RK_BLOCK * SC_ITEMS) + threadIdx.x;
   unsigned k[SC_ITEMS];
   V v[SC_ITEMS];
@@ -425,23 +462,29 @@ void scatter_partitioned(V *d, const V *s, const int *idx, int n, int n_d, vec_p
   unsigned *state = (unsigned *)(mem + L.state);
   const int shift = window_shift(n_d);
   const int tiles = rk_tiles(n);
+  unsigned *unsorted = counter + 1;  // the gate: non-zero when some index exceeds its successor
   GCVL_CK(cudaMemsetAsync(hist, 0, 256 * 4, S.stream));
-  GCVL_CK(cudaMemsetAsync(counter, 0, 4, S.stream));
+  GCVL_CK(cudaMemsetAsync(counter, 0, 8, S.stream));
   GCVL_CK(cudaMemsetAsync(state, 0, rk_state_bytes(n), S.stream));
   int hg = S.sm_count * 4;
   if ((long)hg * RK_BLOCK > n) hg = (n + RK_BLOCK - 1) / RK_BLOCK;
-  k_digit_hist<<<hg, RK_BLOCK, 0, S.stream>>>((const unsigned *)idx, n, shift, hist);
+  k_digit_hist<<<hg, RK_BLOCK, 0, S.stream>>>((const unsigned *)idx, n, shift, hist, unsorted);
   launch_check("k_digit_hist");
   k_rank_digit_starts<<<1, 256, 0, S.stream>>>(hist, 1);
   launch_check("k_rank_digit_starts");
+  // ascending indices (e.g. an interleave): one streaming scatter; otherwise
+  // partition by window, then scatter window by window.  The device decides:
+  // the kernels of the branch not taken return at once.
+  const long g = ((long)n + RK_BLOCK * SC_ITEMS - 1) / (RK_BLOCK * SC_ITEMS);
+  k_sorted_scatter<V><<<(int)g, RK_BLOCK, 0, S.stream>>>(d, s, idx, n, unsorted);
+  launch_check("k_sorted_scatter");
   PassArgs<unsigned, V> a{};
   a.kin = (const unsigned *)idx; a.vin = s;
   a.kout = (unsigned *)(mem + L.kout); a.vout = (V *)(mem + L.vout);
-  a.starts = hist; a.state = state; a.counter = counter;
+  a.starts = hist; a.state = state; a.counter = counter; a.gate = unsorted;
   a.n = n; a.shift = shift; a.status = S.d_status; a.spin_limit = S.spin_limit;
   launch_pass<unsigned, V, false, IN_ARRAYS, OUT_ARRAYS, false>(a, tiles);
-  const long g = ((long)n + RK_BLOCK * SC_ITEMS - 1) / (RK_BLOCK * SC_ITEMS);
-  k_window_scatter<V><<<(int)g, RK_BLOCK, 0, S.stream>>>(d, a.kout, a.vout, n);
+  k_window_scatter<V><<<(int)g, RK_BLOCK, 0, S.stream>>>(d, a.kout, a.vout, n, unsorted);
   launch_check("k_window_scatter");
 }
 template void scatter_partitioned<unsigned>(unsigned *, const unsigned *, const int *, int, int, vec_p);
@@ -578,7 +621,8 @@ void rank_impl(vec_p d, vec_p s, vec_p sd, int n, int m, vec_p scratch, int is_d
     a.n = n; a.shift = shift; a.status = S.d_status; a.spin_limit = S.spin_limit;
     launch_pass<unsigned, unsigned, false, IN_ARRAYS, OUT_ARRAYS, false>(a, tiles);
     const long g = ((long)n + RK_BLOCK * SC_ITEMS - 1) / (RK_BLOCK * SC_ITEMS);
-    k_window_scatter<unsigned><<<(int)g, RK_BLOCK, 0, S.stream>>>((unsigned *)d, iA, (const unsigned *)kA, n);
+    k_window_scatter<unsigned><<<(int)g, RK_BLOCK, 0, S.stream>>>((unsigned *)d, iA, (const unsigned *)kA, n,
+                                                               nullptr);
     launch_check("k_window_scatter");
   }
 }

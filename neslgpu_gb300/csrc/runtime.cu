@@ -124,6 +124,17 @@ GCVL_EXPORT void gcvl_set_stream(void *stream) {
   if (stream) { s.stream = (cudaStream_t)stream; s.own_stream = false; }
   else if (own) { s.stream = own; s.own_stream = true; }
 }
+// A new non-blocking stream on the library's device, for gcvl_set_stream
+// (copies on one stream overlapping kernels on another); NULL on failure.
+GCVL_EXPORT void *gcvl_stream_create(void) {
+  ensure_init();
+  cudaStream_t q = nullptr;
+  if (!GCVL_CK(cudaStreamCreateWithFlags(&q, cudaStreamNonBlocking))) return nullptr;
+  return (void *)q;
+}
+GCVL_EXPORT void gcvl_stream_destroy(void *stream) {
+  if (stream) GCVL_CK(cudaStreamDestroy((cudaStream_t)stream));
+}
 // Number of kernels this library has launched (all entry points).
 GCVL_EXPORT unsigned long long gcvl_launch_count(void) { return gcvl::g_launches; }
 

@@ -259,8 +259,15 @@ k_scan(ScanArgs<typename Op::T> a) {
 #define GCVL_TT 128
 #endif
 constexpr int TT = GCVL_TT;  // threads per CTA = rows per tile
-constexpr int WMAX = 1024;   // offsets window held in shared memory
 template <class T> constexpr int row_items() { return 128 / (int)sizeof(T); }
+// Offsets window of a segmented reduction, held in shared memory: room for
+// every segment of a tile whose segments average at least one element
+// (float64) or two (int; a bigger window would cost an int reduction its
+// seventh CTA per SM).  Tiles with more segments look offsets up in global
+// memory.  Scans keep no window.
+template <class T, int MODE> constexpr int wmax() {
+  return MODE == M_REDUCE ? TT * row_items<T>() / (int)(8 / sizeof(T)) + 2 : 0;
+}
 
 template <class T> struct TArgs {
   T *out;
@@ -418,7 +425,7 @@ __global__ void __launch_bounds__(TB_LB, MODE == M_REDUCE ? (sizeof(typename Op:
     const long e = base + valid;
     const int sl = (e >= a.n) ? a.sv.m - 1 : __ldg(a.sv.gran + e / kGranule);
     W = sl - sf + 2;
-    if (W <= WMAX)
+    if (W <= wmax<T, MODE>())
       for (int i = tid; i < W; i += TT) win[i] = __ldg(a.sv.off + sf + i);
     named_sync(2, TT);  // window loaded
   }
@@ -428,7 +435,7 @@ __global__ void __launch_bounds__(TB_LB, MODE == M_REDUCE ? (sizeof(typename Op:
       if (++it >= a.spin_limit) { atomicOr(a.status, DEV_TIMEOUT); break; }
     }
   }
-  const OffWin off{win, a.sv.off, sf, (SEG && W <= WMAX) ? W : 0};
+  const OffWin off{win, a.sv.off, sf, (SEG && W <= wmax<T, MODE>()) ? W : 0};
 
   // this thread's row
   const long grow = (long)tile * TT + tid;
@@ -450,7 +457,7 @@ __global__ void __launch_bounds__(TB_LB, MODE == M_REDUCE ? (sizeof(typename Op:
   // segment holding k0 (reductions): the last window entry <= k0
   int s0 = 0;
   if (SEG && MODE == M_REDUCE && cnt > 0) {
-    if (W <= WMAX) {
+    if (W <= wmax<T, MODE>()) {
       int lo = 0, hi = W - 2;
       while (lo < hi) {
         int mid = (lo + hi + 1) >> 1;
@@ -700,7 +707,9 @@ inline size_t reduce_pass_bytes(int tiles) {
   const int chunks = (tiles + 1023) / 1024;
   return lookback_bytes(tiles) + align_up((size_t)tiles * 4, 256) + lookback_bytes(chunks);
 }
-template <class T> constexpr size_t tma_smem() { return 1024 + (size_t)TT * row_items<T>() * sizeof(T) + WMAX * 4; }
+template <class T, int MODE> constexpr size_t tma_smem() {
+  return 1024 + (size_t)TT * row_items<T>() * sizeof(T) + (size_t)wmax<T, MODE>() * 4;
+}
 
 // Returns false (nothing launched) when the vectors do not suit TMA.
 template <class Op, int MODE, bool SEG>
@@ -727,7 +736,7 @@ bool run_scan_tma(typename Op::T *out, const typename Op::T *in, vec_p sd, int n
   a.lead = (int *)((char *)a.lb.word + align_up((size_t)tiles * 16, 256));
   GCVL_CK(cudaMemsetAsync(mem, 0, lookback_clear_bytes(tiles), S.stream));
   if (MODE == M_REDUCE) GCVL_CK(cudaMemsetAsync(a.lead, 0xFF, (size_t)tiles * 4, S.stream));
-  k_scan_tma<Op, MODE, SEG><<<tiles, TB_LB, tma_smem<T>(), S.stream>>>(tin, tout, a);
+  k_scan_tma<Op, MODE, SEG><<<tiles, TB_LB, tma_smem<T, MODE>(), S.stream>>>(tin, tout, a);
   launch_check(name);
   if (MODE == M_REDUCE && tiles > 1) {
     const int chunks = ceil_div(tiles, FIX_NT);
@@ -1142,8 +1151,8 @@ GCVL_EXPORT int gcvl_add_sed_noalloc(vec_p d, vec_p s, vec_p sd, int n, int m) {
     a.lb = lookback_carve(mem, tiles);
     a.status = g_noalloc_status_ptr[dev];
     a.spin_limit = S.spin_limit;
-    if (seg) k_scan_tma<AddD, M_SCAN, true><<<tiles, TB_LB, tma_smem<double>(), strm>>>(tin, tout, a);
-    else k_scan_tma<AddD, M_SCAN, false><<<tiles, TB_LB, tma_smem<double>(), strm>>>(tin, tout, a);
+    if (seg) k_scan_tma<AddD, M_SCAN, true><<<tiles, TB_LB, tma_smem<double, M_SCAN>(), strm>>>(tin, tout, a);
+    else k_scan_tma<AddD, M_SCAN, false><<<tiles, TB_LB, tma_smem<double, M_SCAN>(), strm>>>(tin, tout, a);
   } else {
     ScanArgs<double> a;
     a.out = out; a.in = in; a.out2 = nullptr; a.n = n;

@@ -11,6 +11,10 @@
 // unspecified here (the serial CVL keeps the last writer).
 #include "gcvl.cuh"
 
+// the library's own +-scan (scan.cu), used for the pack's tile offsets
+extern "C" void add_suz(vec_p d, vec_p s, int len, vec_p scratch);
+extern "C" int add_suz_scratch(int len);
+
 namespace gcvl {
 
 constexpr int VBLOCK = 256;
@@ -109,6 +113,56 @@ template <class F> void segmap(F f, const SegView &sv, const char *name) {
   k_segmap<F><<<(int)((sv.n + per - 1) / per), SMB, 0, stream()>>>(f, sv);
   launch_check(name);
 }
+// Segmented permute, d[start(seg(k)) + i[k]] = s[k]: a warp owns SMI*32
+// consecutive elements; each lane walks SMI consecutive ones through the
+// segment descriptor and records their segment starts in shared memory;
+// then the index and value loads are coalesced (element j*32 + lane) and
+// all of a lane's stores are in flight together.
+template <class T>
+__global__ void __launch_bounds__(SMB) k_segscatter(T *__restrict__ d, const T *__restrict__ s,
+                                                    const int *__restrict__ idx, SegView sv) {
+  constexpr int WE = 32 * SMI, PADW = WE + 32;
+  __shared__ int s_start[SMB / 32][PADW];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const long wbase = ((long)blockIdx.x * (SMB / 32) + warp) * WE;
+  if (wbase >= sv.n) return;
+  const int wcnt = (int)min((long)WE, (long)sv.n - wbase);
+  // index and value loads issued before the walk, so that they overlap it
+  int ix[SMI];
+  T v[SMI];
+#pragma unroll
+  for (int j = 0; j < SMI; j++) {
+    const int e = j * 32 + lane;
+    if (e < wcnt) { ix[j] = __ldcs(idx + wbase + e); v[j] = __ldcs(s + wbase + e); }
+  }
+  const int e0 = lane * SMI;
+  const int cnt = max(0, min(SMI, wcnt - e0));
+  if (cnt > 0) {
+    const int k0 = (int)(wbase + e0);
+    int sg = seg_of(sv, k0);
+    int start = __ldg(sv.off + sg), end = __ldg(sv.off + sg + 1);
+#pragma unroll
+    for (int i = 0; i < SMI; i++) {
+      if (i < cnt) {
+        while (k0 + i >= end) { ++sg; start = end; end = __ldg(sv.off + sg + 1); }
+        s_start[warp][e0 + lane + i] = start;  // element e at e + e / SMI
+      }
+    }
+  }
+  __syncwarp();
+#pragma unroll
+  for (int j = 0; j < SMI; j++) {
+    const int e = j * 32 + lane;
+    if (e < wcnt) d[(long)s_start[warp][e + e / SMI] + ix[j]] = v[j];
+  }
+}
+template <class T> void segscatter(T *d, const T *s, const int *idx, const SegView &sv, const char *name) {
+  if (sv.n <= 0 || sv.m <= 0) return;
+  const long per = (long)SMB * SMI;
+  k_segscatter<T><<<(int)((sv.n + per - 1) / per), SMB, 0, stream()>>>(d, s, idx, sv);
+  launch_check(name);
+}
+
 template <class TT> struct DisMap {  // d[k] = v[seg(k)]
   typedef TT T;
   static constexpr bool AUX = false, GATHER = false;
@@ -367,11 +421,137 @@ __global__ void __launch_bounds__(PBLOCK) k_pack(T *__restrict__ d, const T *__r
   for (int e = tid; e < cnt; e += PBLOCK) d[out0 + e] = s_val[e];
 }
 
+// Pack of long vectors in two passes, no tile waiting for another (at large
+// n the one-pass kernel's look-back chain, not HBM, bounds it).  Pass 1
+// reads the flags once, writes them as a bit mask (element k: bit k&31 of
+// word k>>5) and every tile's count of true flags; an exclusive +-scan of
+// the counts gives each tile its output offset; pass 2 reads the mask (one
+// bit per element instead of the 4-byte flag) and the values, and writes
+// each tile's kept values as one coalesced run.
+constexpr int PACK_TWO_PASS_TILES = 64;
+constexpr int PWORDS = PTILE / 32;  // mask words per tile
+
+__global__ void __launch_bounds__(PBLOCK) k_pack_count(const int *__restrict__ f, int n,
+                                                      unsigned *__restrict__ bits, int *__restrict__ cnt) {
+  __shared__ unsigned s_bits[PWORDS];
+  __shared__ int s_c[PBLOCK / 32];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const long base = (long)blockIdx.x * PTILE;
+  const int valid = (int)min((long)PTILE, (long)n - base);
+  int fl[PITEMS];
+#pragma unroll
+  for (int j = 0; j < PITEMS; j++) {
+    const int e = j * PBLOCK + tid;
+    fl[j] = e < valid ? __ldcs(f + base + e) : 0;
+  }
+  int c = 0;
+#pragma unroll
+  for (int j = 0; j < PITEMS; j++) {
+    // elements j*PBLOCK + warp*32 + lane: mask word j*8 + warp of the tile
+    const unsigned b = __ballot_sync(0xffffffffu, fl[j] != 0);
+    if (lane == 0) s_bits[j * (PBLOCK / 32) + warp] = b;
+    c += __popc(b);
+  }
+  if (lane == 0) s_c[warp] = c;
+  __syncthreads();
+  const int nw = (valid + 31) >> 5;
+  if (tid < nw) bits[(base >> 5) + tid] = s_bits[tid];
+  if (tid == 0) {
+    int t = 0;
+#pragma unroll
+    for (int w = 0; w < PBLOCK / 32; w++) t += s_c[w];
+    cnt[blockIdx.x] = t;
+  }
+}
+
+template <class T>
+__global__ void __launch_bounds__(PBLOCK) k_pack_place(T *__restrict__ d, const T *__restrict__ s,
+                                                      const unsigned *__restrict__ bits,
+                                                      const int *__restrict__ offs, int n) {
+  __shared__ T s_val[PTILE];
+  __shared__ unsigned s_word[PWORDS];
+  __shared__ int s_wpre[PWORDS + 1];
+  __shared__ int s_ws[PWORDS / 32];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const long base = (long)blockIdx.x * PTILE;
+  const int valid = (int)min((long)PTILE, (long)n - base);
+  // the values' loads first, kept in registers while the mask is ranked
+  T vals[PITEMS];
+#pragma unroll
+  for (int j = 0; j < PITEMS; j++) {
+    const int e = j * PBLOCK + tid;
+    if (e < valid) vals[j] = __ldcs(s + base + e);
+  }
+  const long out0 = __ldg(offs + blockIdx.x);
+  // exclusive prefix of the words' popcounts (threads 0..PWORDS-1, one word each)
+  if (tid < PWORDS) {
+    const int nw = (valid + 31) >> 5;
+    const unsigned w = tid < nw ? __ldg(bits + (base >> 5) + tid) : 0u;
+    const int c = __popc(w);
+    int incl = c;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int x = shfl_up(incl, o);
+      if (lane >= o) incl += x;
+    }
+    if (lane == 31) s_ws[warp] = incl;
+    s_word[tid] = w;
+    s_wpre[tid] = incl - c;
+  }
+  __syncthreads();
+  if (tid < PWORDS) {
+    int p = 0;
+#pragma unroll
+    for (int w = 0; w < PWORDS / 32; w++) if (w < warp) p += s_ws[w];
+    s_wpre[tid] += p;
+    if (tid == PWORDS - 1) s_wpre[PWORDS] = p + s_ws[warp];
+  }
+  __syncthreads();
+  const unsigned lt = (1u << lane) - 1u;
+#pragma unroll
+  for (int j = 0; j < PITEMS; j++) {
+    const int e = j * PBLOCK + tid;
+    const int wi = e >> 5;  // == j * 8 + warp: one word per warp and step
+    const unsigned w = s_word[wi];
+    if (e < valid && ((w >> lane) & 1u)) s_val[s_wpre[wi] + __popc(w & lt)] = vals[j];
+  }
+  __syncthreads();
+  const int total = s_wpre[PWORDS];
+  for (int e = tid; e < total; e += PBLOCK) __stcs(d + out0 + e, s_val[e]);
+}
+
+struct PackLayout { size_t bits, cnt, offs, scan, total; };
+inline PackLayout pack_layout(int n) {
+  const int tiles = ceil_div(n, PTILE);
+  PackLayout L;
+  size_t o = 0;
+  auto take = [&](size_t bytes) { size_t at = o; o += align_up(bytes, 256); return at; };
+  L.bits = take((size_t)ceil_div(n, 32) * 4);
+  L.cnt = take((size_t)tiles * 4);
+  L.offs = take((size_t)tiles * 4);
+  L.scan = take((size_t)add_suz_scratch(tiles) * 8);
+  L.total = o;
+  return L;
+}
+
 template <class T> void pack(vec_p d, vec_p s, vec_p f, int n, vec_p scratch, const char *name) {
   ensure_init();
   State &S = st();
   if (n <= 0) return;
   int tiles = ceil_div(n, PTILE);
+  if (tiles >= PACK_TWO_PASS_TILES) {
+    const PackLayout L = pack_layout(n);
+    char *mem = (char *)scratch_or_work(scratch, L.total);
+    if (!mem) return;
+    unsigned *bits = (unsigned *)(mem + L.bits);
+    int *cnt = (int *)(mem + L.cnt), *offs = (int *)(mem + L.offs);
+    k_pack_count<<<tiles, PBLOCK, 0, S.stream>>>((const int *)f, n, bits, cnt);
+    launch_check(name);
+    add_suz(offs, cnt, tiles, mem + L.scan);
+    k_pack_place<T><<<tiles, PBLOCK, 0, S.stream>>>((T *)d, (const T *)s, bits, offs, n);
+    launch_check(name);
+    return;
+  }
   void *mem = scratch_or_work(scratch, lookback_bytes(tiles));
   if (!mem) return;
   LookbackMem lb = lookback_carve(mem, tiles);
@@ -380,7 +560,12 @@ template <class T> void pack(vec_p d, vec_p s, vec_p f, int n, vec_p scratch, co
                                             S.spin_limit);
   launch_check(name);
 }
-int pack_units(int n) { return n <= 0 ? 0 : lookback_units(ceil_div(n, PTILE)); }
+int pack_units(int n) {
+  if (n <= 0) return 0;
+  const int tiles = ceil_div(n, PTILE);
+  if (tiles >= PACK_TWO_PASS_TILES) return (int)((pack_layout(n).total + 7) / 8);
+  return lookback_units(tiles);
+}
 
 }  // namespace gcvl
 
@@ -477,7 +662,7 @@ META_SEG(ind_lez, INPLACE_NONE)
                              vec_p scratch) {                                           \
     ensure_init();                                                                      \
     if (m == 1) { scatter<T>((T *)d, (const T *)s, (const int *)i, n, n, scratch, "smp_pe" #L); return; } \
-    segwalk(PermSeg<T>{(T *)d, (const T *)s, (const int *)i}, seg_view(sd, n, m), "smp_pe" #L); \
+    segscatter<T>((T *)d, (const T *)s, (const int *)i, seg_view(sd, n, m), "smp_pe" #L); \
   }                                                                                     \
   GCVL_EXPORT int smp_pe##L##_scratch(int n, int m) { return m == 1 ? scatter_units<T>(n, n) : 0; } \
   GCVL_EXPORT unsigned smp_pe##L##_inplace(void) { return INPLACE_NONE; }               \

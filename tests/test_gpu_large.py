@@ -78,3 +78,70 @@ def test_segmented_reductions_many_chunks(gpu, oracle, kind):
     for name, x in (("add_rez", xi), ("max_rez", xi), ("min_red", xd)):
         compare("exact", ops.reduce_e(gpu, name, x, lens), ops.reduce_e(oracle, name, x, lens))
     compare("exact", ops.pk1_e(gpu, fl, lens), ops.pk1_e(oracle, fl, lens))
+
+
+def test_default_permute_ascending_indices(gpu, oracle, data):
+    """Ascending indices (the interleave of a flattened three-way split):
+    the partitioned scatter's device-side check sends them to one streaming
+    scatter instead of the window partition."""
+    nd = 3 * N
+    idx = (3 * np.arange(N, dtype=np.int64) + 1).astype(np.int32)
+    dflt = np.full(nd, -3, dtype=np.int32)
+    compare("exact", ops.dpe_u(gpu, "dpe_puz", data["xi"], idx, dflt),
+            ops.dpe_u(oracle, "dpe_puz", data["xi"], idx, dflt))
+    ident = np.arange(N, dtype=np.int32)
+    compare("exact", ops.smp_u(gpu, "smp_pud", data["xd"], ident), ops.smp_u(oracle, "smp_pud", data["xd"], ident))
+    # one descent breaks the order: the partitioned path again
+    idx2 = ident.copy()
+    idx2[N // 2], idx2[N // 2 + 1] = idx2[N // 2 + 1], idx2[N // 2]
+    compare("exact", ops.smp_u(gpu, "smp_puz", data["xi"], idx2), ops.smp_u(oracle, "smp_puz", data["xi"], idx2))
+
+
+@pytest.mark.parametrize("t", ["z", "d"])
+def test_pack_two_pass(gpu, oracle, data, t):
+    """Packs long enough for the two-pass form (flag mask and tile counts,
+    then placement at scanned tile offsets), unsegmented and segmented,
+    sparse and dense flags."""
+    x = data["xi"] if t == "z" else data["xd"]
+    r = W.rng(17)
+    for p in (0.5, 0.01, 0.999):
+        fl = (r.random(N) < p).astype(np.int32)
+        compare("exact", ops.pack_u(gpu, f"pk2_lu{t}", x, fl), ops.pack_u(oracle, f"pk2_lu{t}", x, fl))
+    fl = (r.random(N) < 0.3).astype(np.int32)
+    g, gl = ops.pack_e(gpu, f"pk2_le{t}", x, fl, data["lens"])
+    o, ol = ops.pack_e(oracle, f"pk2_le{t}", x, fl, data["lens"])
+    compare("exact", gl, ol)
+    compare("exact", g, o)
+
+
+@pytest.mark.parametrize("t", ["z", "d"])
+def test_segmented_permute_many_segments(gpu, oracle, data, t):
+    """PERMUTE within every segment (the coalesced segmented scatter), short
+    and empty segments included."""
+    x = data["xi"] if t == "z" else data["xd"]
+    r = W.rng(23)
+    lens = W.with_empty(r, W.geometric_lengths(r, N, 3.0), 0.1)
+    # a random permutation of every segment: rank of a random key within the segment
+    seg = np.repeat(np.arange(len(lens)), lens)
+    start = np.concatenate([[0], np.cumsum(lens, dtype=np.int64)[:-1]])
+    order = np.lexsort((r.random(N), seg))
+    idx = np.empty(N, dtype=np.int32)
+    idx[order] = (np.arange(N) - start[seg[order]]).astype(np.int32)
+    compare("exact", ops.smp_e(gpu, f"smp_pe{t}", x, idx, lens), ops.smp_e(oracle, f"smp_pe{t}", x, idx, lens))
+
+
+@pytest.mark.parametrize("mean", [1.0, 1.7, 2.5])
+def test_reductions_tiny_segments(gpu, oracle, mean):
+    """Segmented reductions whose tiles hold as many segments as elements
+    (the shared-memory offsets window) or more (empty segments: global
+    offsets)."""
+    from cases import seg_abs_total
+    r = W.rng(int(mean * 10))
+    n = (1 << 21) + 3
+    lens = W.with_empty(r, W.geometric_lengths(r, n, mean), 0.2)
+    xi = r.integers(-1000, 1000, size=n).astype(np.int32)
+    xd = W.float64_normal(r, n)
+    for name, x in (("min_rez", xi), ("max_rez", xi), ("add_rez", xi), ("max_red", xd)):
+        compare("exact", ops.reduce_e(gpu, name, x, lens), ops.reduce_e(oracle, name, x, lens))
+    compare("sum", ops.reduce_e(gpu, "add_red", xd, lens), ops.reduce_e(oracle, "add_red", xd, lens),
+            seg_abs_total(xd, lens))
