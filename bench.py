@@ -13,10 +13,11 @@ Printed as one JSON line (rank 0).  Besides the headline it carries:
                   the measured HBM copy bandwidth of MEASURED_PEAKS.json
   e2e          -- the same step through the C ABI with pinned host buffers,
                   every step uploading the values and downloading both
-                  results: the vector cut at segment starts into 8 pieces
-                  on two library streams, so that one piece's transfers
-                  overlap another's kernels ("sequential": whole-vector
-                  c2v_fud, both primitives, v2c_fud x2)
+                  results: the vector cut at segment starts into 8 pieces,
+                  pipelined on three streams (uploads, kernels, downloads)
+                  so that transfers in both directions and kernels overlap
+                  ("sequential": whole-vector c2v_fud, both primitives,
+                  v2c_fud x2)
   cpu_baseline -- the CPU oracle (plain-C restatement of the serial CVL)
                   on one host core over the same workload
   primitives   -- Gelem/s and roofline fraction of the other CVL primitives
@@ -463,10 +464,12 @@ def e2e_pipelined(g, lens, hx, hs, hr, steps, chunks=8):
     """The end-to-end step with the vector cut at segment starts into
     `chunks` pieces of about n / chunks elements, each a segmented vector of
     its own (device buffers and segment descriptor built once, outside the
-    timed region), issued on two library streams in turn: the upload of one
-    piece, the kernels of another and the download of a third overlap.
-    Every element and segment goes up and comes back exactly once per step.
-    Returns (seconds per step, pieces)."""
+    timed region), as a three-stage pipeline on three library streams --
+    uploads, kernels, downloads -- ordered by events, so that the upload of
+    one piece, the kernels of another and the download of a third overlap
+    (and uploads overlap downloads: the link carries both directions at
+    once).  Every element and segment goes up and comes back exactly once
+    per step.  Returns (seconds per step, pieces)."""
     c = g.c
     n = int(lens.sum())
     ends = np.cumsum(lens, dtype=np.int64)
@@ -490,18 +493,36 @@ def e2e_pipelined(g, lens, hx, hs, hr, steps, chunks=8):
         pieces.append(p)
         s0 = s1
     assert sum(p["n"] for p in pieces) == n and sum(p["m"] for p in pieces) == len(lens)
-    streams = [c.gcvl_stream_create() for _ in range(2)]
+    streams = [c.gcvl_stream_create() for _ in range(3)]
     if not all(streams):
         raise RuntimeError(c.gcvl_error_string().decode())
+    up, ker, down = streams
+    for p in pieces:
+        p["ev"] = {k: c.gcvl_event_create() for k in ("up", "ker", "down")}
+        c.gcvl_set_stream(ker)
+        c.gcvl_event_record(p["ev"]["ker"])
+        c.gcvl_event_record(p["ev"]["down"])
+    c.gcvl_set_stream(None)
 
     def run():
-        for i, p in enumerate(pieces):
-            c.gcvl_set_stream(streams[i % 2])
+        for p in pieces:
+            ev = p["ev"]
+            c.gcvl_set_stream(up)
+            c.gcvl_stream_wait_event(ev["ker"])  # the previous step's kernels have read x
             c.gcvl_h2d_async(p["x"], hx + 8 * p["e0"], 8 * p["n"])
+            c.gcvl_event_record(ev["up"])
+            c.gcvl_set_stream(ker)
+            c.gcvl_stream_wait_event(ev["up"])
+            c.gcvl_stream_wait_event(ev["down"])  # the previous step's downloads have read y, r
             c.add_sed(p["y"], p["x"], p["sd"], p["n"], p["m"], p["scr"])
             c.add_red(p["r"], p["x"], p["sd"], p["n"], p["m"], p["scr"])
+            c.gcvl_event_record(ev["ker"])
+            c.gcvl_set_stream(down)
+            c.gcvl_stream_wait_event(ev["ker"])
             c.gcvl_d2h_async(hs + 8 * p["e0"], p["y"], 8 * p["n"])
             c.gcvl_d2h_async(hr + 8 * p["s0"], p["r"], 8 * p["m"])
+            c.gcvl_event_record(ev["down"])
+        c.gcvl_set_stream(None)
 
     def sync_all():
         for q in streams:
@@ -526,6 +547,8 @@ def e2e_pipelined(g, lens, hx, hs, hr, steps, chunks=8):
     for p in pieces:
         for k in ("x", "y", "r", "sd", "scr"):
             c.fre_fov(p[k])
+        for e in p["ev"].values():
+            c.gcvl_event_destroy(e)
     return dt, len(pieces)
 
 
@@ -650,8 +673,8 @@ def gpu_arm(a):
                "ms_per_step": round(dt_pipe * 1e3, 3),
                "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n + 8 * m,
                "api": f"gcvl_h2d_async, add_sed, add_red, gcvl_d2h_async x2 per piece; {npieces} pieces cut at "
-                      "segment starts, two library streams (gcvl_stream_create / gcvl_set_stream), "
-                      "pinned host buffers",
+                      "segment starts, pipelined on three library streams (uploads, kernels, downloads; "
+                      "gcvl_stream_create / gcvl_set_stream / gcvl_stream_wait_event), pinned host buffers",
                "max_abs_diff_vs_whole_vector": diff,
                "sequential": {"value": round(world * 2 * n / dt_seq / 1e9, 3), "ms_per_step": round(dt_seq * 1e3, 3),
                               "api": "c2v_fud, add_sed, add_red, v2c_fud x2 on the whole vector"}}

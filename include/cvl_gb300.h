@@ -739,6 +739,9 @@ void *gcvl_event_create(void);
 void gcvl_event_record(void *event);
 float gcvl_event_elapsed_ms(void *start, void *stop);
 void gcvl_event_destroy(void *event);
+/* Make later work on the library stream wait for the event's last record
+ * (on any stream).  No counterpart in the reference (one implicit stream). */
+void gcvl_stream_wait_event(void *event);
 /* Pinned host memory and asynchronous transfers on the library stream. */
 void *gcvl_host_alloc(size_t bytes);
 void gcvl_host_free(void *p);

@@ -196,6 +196,12 @@ GCVL_EXPORT float gcvl_event_elapsed_ms(void *a, void *b) {
   return ms;
 }
 GCVL_EXPORT void gcvl_event_destroy(void *e) { cudaEventDestroy((cudaEvent_t)e); }
+// Later work on the library stream waits for the event's last record (on
+// any stream): orders a pipeline whose stages run on different streams.
+GCVL_EXPORT void gcvl_stream_wait_event(void *e) {
+  ensure_init();
+  GCVL_CK(cudaStreamWaitEvent(st().stream, (cudaEvent_t)e, 0));
+}
 
 // Pinned host memory for callers that time host<->device transfers.
 GCVL_EXPORT void *gcvl_host_alloc(size_t bytes) {
