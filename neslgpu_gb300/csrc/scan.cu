@@ -330,13 +330,17 @@ template <int ITEMS> struct Engine<AddD, ITEMS> {
 };
 
 // Reductions: a thread's float64 + fold split between the integer pipes
-// (first half of its items, fixed point) and the FP64 pipe (second half, an
-// add chain), so that neither carries the whole fold.  The segmented
-// reduction has no per-element output work to keep the FP64 pipe busy.
+// (the first GCVL_RED_FX_ITEMS items, fixed point) and the FP64 pipe (the
+// rest, an add chain), so that neither carries the whole fold; 12 of 16
+// measured best (2 % over 8 of 16).  The segmented reduction has no
+// per-element output work to keep the FP64 pipe busy.
+#ifndef GCVL_RED_FX_ITEMS
+#define GCVL_RED_FX_ITEMS 12
+#endif
 template <int ITEMS>
 __device__ __forceinline__ void agg_add_split(const double (&x)[ITEMS], unsigned heads, int cnt, int &tf,
                                               double &tv) {
-  constexpr int H = ITEMS / 2;
+  constexpr int H = GCVL_RED_FX_ITEMS < ITEMS ? GCVL_RED_FX_ITEMS : ITEMS;  // items in fixed point
   tf = heads != 0;
   tv = AddD::ident();
   if (cnt <= 0) return;
@@ -356,8 +360,19 @@ __device__ __forceinline__ void agg_add_split(const double (&x)[ITEMS], unsigned
 // following them.  The compute warps publish the tile aggregate as soon as it
 // exists and meet the look-back warp only when they need the carry.
 constexpr int TB_LB = TT + 32;  // threads per CTA
+// resident CTAs per SM the register allocation must allow (scans hold no
+// offsets window, so registers, not shared memory, set their occupancy)
+#ifndef GCVL_SCAN_MINB
+#define GCVL_SCAN_MINB 5
+#endif
+#ifndef GCVL_RED_MINB_D
+#define GCVL_RED_MINB_D 6
+#endif
+#ifndef GCVL_RED_MINB_Z
+#define GCVL_RED_MINB_Z 7
+#endif
 template <class Op, int MODE, bool SEG>
-__global__ void __launch_bounds__(TB_LB, MODE == M_REDUCE ? (sizeof(typename Op::T) == 8 ? 6 : 7) : 5) k_scan_tma(const __grid_constant__ CUtensorMap tin,
+__global__ void __launch_bounds__(TB_LB, MODE == M_REDUCE ? (sizeof(typename Op::T) == 8 ? GCVL_RED_MINB_D : GCVL_RED_MINB_Z) : GCVL_SCAN_MINB) k_scan_tma(const __grid_constant__ CUtensorMap tin,
                                                      const __grid_constant__ CUtensorMap tout,
                                                      TArgs<typename Op::T> a) {
   typedef typename Op::T T;

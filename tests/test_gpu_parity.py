@@ -51,3 +51,10 @@ def test_parity_unaligned_vectors(oracle, kind):
     if not _has_gpu():
         pytest.skip("no GPU")
     _run_all(DeviceRunner(load(), offset=1), oracle, 70_001, kind, seed=21)
+
+
+@pytest.mark.parametrize("kind", ["long", "tiny", "empty", "one"])
+def test_parity_two_million(gpu, oracle, kind):
+    """Every primitive past 2^21 elements (a thousand tiles and more):
+    segments spanning many tiles, tiny and empty segments, one segment."""
+    _run_all(gpu, oracle, (1 << 21) + 13, kind, seed=31)
