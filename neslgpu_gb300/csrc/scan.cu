@@ -360,13 +360,17 @@ __device__ __forceinline__ void agg_add_split(const double (&x)[ITEMS], unsigned
 // following them.  The compute warps publish the tile aggregate as soon as it
 // exists and meet the look-back warp only when they need the carry.
 constexpr int TB_LB = TT + 32;  // threads per CTA
-// resident CTAs per SM the register allocation must allow (scans hold no
-// offsets window, so registers, not shared memory, set their occupancy)
+// Resident CTAs per SM the register allocation must allow.  Scans hold no
+// offsets window, so registers, not shared memory, set their occupancy: 8
+// (48-56 registers, a few spilled) measured 4 % faster than 7 on the float64
+// scan and 27 % on the int scan; 9 spills heavily and is slower.  Float64
+// reductions: 7 (their window leaves room for 8 by shared memory, but 8
+// spills).
 #ifndef GCVL_SCAN_MINB
-#define GCVL_SCAN_MINB 5
+#define GCVL_SCAN_MINB 8
 #endif
 #ifndef GCVL_RED_MINB_D
-#define GCVL_RED_MINB_D 6
+#define GCVL_RED_MINB_D 7
 #endif
 #ifndef GCVL_RED_MINB_Z
 #define GCVL_RED_MINB_Z 7
