@@ -53,6 +53,7 @@ sys.path.insert(0, str(ROOT))
 LOG2N = 28
 SEED = 0x5EED + 1
 METRIC = "CVL primitive Gelem/s (segmented +_scan and +_reduce, float64)"
+NCU_SCAN_DRAM_BYTES_PER_ELEM = 503.19e6 / (1 << 25)  # add_sed's DRAM traffic per element, ncu at 2^25
 UNIT = "Gelem/s"
 
 
@@ -619,16 +620,14 @@ def gpu_arm(a):
     # roofline of the dominant kernel (the add_sed scan)
     alg_bytes = 16.0 * n + 4.0 * m
     achieved = alg_bytes / (t_sed * 1e-3) / 1e9
-    traffic = None
-    tf = ROOT / "profiles" / "ncu_traffic.json"
-    if tf.exists():
-        try:
-            traffic = json.loads(tf.read_text()).get("add_sed_bytes_per_launch")
-        except (ValueError, OSError):
-            traffic = None
-    roofline = {"bound": "hbm", "kernel": "k_scan<AddD,scan,segmented> (add_sed)",
+    # DRAM bytes per launch: dram__bytes_read.sum + dram__bytes_write.sum of
+    # one ncu capture of this kernel at 2^25 elements (503 MB), scaled by the
+    # elements to this launch (profiles/k_scan_tma_add_sed_add_red_2e25.md)
+    traffic = round(NCU_SCAN_DRAM_BYTES_PER_ELEM * n)
+    roofline = {"bound": "hbm", "kernel": "k_scan_tma<AddD,scan,segmented> (add_sed)",
                 "achieved": round(achieved, 1), "peak": hbm, "peak_kind": peak_kind, "unit": "GB/s",
                 "frac": round(achieved / hbm, 4), "traffic": traffic,
+                "traffic_source": "ncu capture at 2^25 elements, scaled by the elements",
                 "alg_bytes_per_launch": alg_bytes,
                 "add_red": {"ms": round(t_red, 4),
                             "achieved": round((8.0 * n + 12.0 * m) / (t_red * 1e-3) / 1e9, 1)}}
