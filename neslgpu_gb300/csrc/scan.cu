@@ -260,13 +260,18 @@ k_scan(ScanArgs<typename Op::T> a) {
 #endif
 constexpr int TT = GCVL_TT;  // threads per CTA = rows per tile
 template <class T> constexpr int row_items() { return 128 / (int)sizeof(T); }
-// Offsets window of a segmented reduction, held in shared memory: room for
-// every segment of a tile whose segments average at least one element
-// (float64) or two (int; a bigger window would cost an int reduction its
-// seventh CTA per SM).  Tiles with more segments look offsets up in global
-// memory.  Scans keep no window.
-template <class T, int MODE> constexpr int wmax() {
-  return MODE == M_REDUCE ? TT * row_items<T>() / (int)(8 / sizeof(T)) + 2 : 0;
+// Offsets window of a segmented reduction, held in shared memory (scans
+// keep none).  Full: room for every segment of a tile whose segments are
+// non-empty.  An int reduction whose segments average 3 elements or more
+// gets half of that (tiles of segments averaging 2 and more fit), keeping
+// its seventh CTA per SM: a full window cost 7 % on long segments, a half
+// one 10x on the one-element segments of a quicksort's last levels.  Tiles
+// with more segments than their window look offsets up in global memory.
+template <class T> constexpr int wmax_full() { return TT * row_items<T>() + 2; }
+template <class T, int MODE> inline int wmax_for(int n, int m) {
+  if (MODE != M_REDUCE) return 0;
+  if (sizeof(T) == 8 || (long)n < 3L * m) return wmax_full<T>();
+  return TT * row_items<T>() / 2 + 2;
 }
 
 template <class T> struct TArgs {
@@ -279,6 +284,7 @@ template <class T> struct TArgs {
   unsigned *status;
   int spin_limit;
   int *lead;  // reductions: per tile, the segment whose result lacks the earlier tiles' part (-1: none)
+  int wmax;   // reductions: entries of the shared-memory offsets window
 };
 
 // Segment offsets seen through the shared-memory window when possible.
@@ -444,7 +450,7 @@ __global__ void __launch_bounds__(TB_LB, MODE == M_REDUCE ? (sizeof(typename Op:
     const long e = base + valid;
     const int sl = (e >= a.n) ? a.sv.m - 1 : __ldg(a.sv.gran + e / kGranule);
     W = sl - sf + 2;
-    if (W <= wmax<T, MODE>())
+    if (W <= a.wmax)
       for (int i = tid; i < W; i += TT) win[i] = __ldg(a.sv.off + sf + i);
     named_sync(2, TT);  // window loaded
   }
@@ -454,7 +460,7 @@ __global__ void __launch_bounds__(TB_LB, MODE == M_REDUCE ? (sizeof(typename Op:
       if (++it >= a.spin_limit) { atomicOr(a.status, DEV_TIMEOUT); break; }
     }
   }
-  const OffWin off{win, a.sv.off, sf, (SEG && W <= wmax<T, MODE>()) ? W : 0};
+  const OffWin off{win, a.sv.off, sf, (SEG && W <= a.wmax) ? W : 0};
 
   // this thread's row
   const long grow = (long)tile * TT + tid;
@@ -476,7 +482,7 @@ __global__ void __launch_bounds__(TB_LB, MODE == M_REDUCE ? (sizeof(typename Op:
   // segment holding k0 (reductions): the last window entry <= k0
   int s0 = 0;
   if (SEG && MODE == M_REDUCE && cnt > 0) {
-    if (W <= wmax<T, MODE>()) {
+    if (W <= a.wmax) {
       int lo = 0, hi = W - 2;
       while (lo < hi) {
         int mid = (lo + hi + 1) >> 1;
@@ -726,8 +732,8 @@ inline size_t reduce_pass_bytes(int tiles) {
   const int chunks = (tiles + 1023) / 1024;
   return lookback_bytes(tiles) + align_up((size_t)tiles * 4, 256) + lookback_bytes(chunks);
 }
-template <class T, int MODE> constexpr size_t tma_smem() {
-  return 1024 + (size_t)TT * row_items<T>() * sizeof(T) + (size_t)wmax<T, MODE>() * 4;
+template <class T> constexpr size_t tma_smem(int wmax) {
+  return 1024 + (size_t)TT * row_items<T>() * sizeof(T) + (size_t)wmax * 4;
 }
 
 // Returns false (nothing launched) when the vectors do not suit TMA.
@@ -755,7 +761,8 @@ bool run_scan_tma(typename Op::T *out, const typename Op::T *in, vec_p sd, int n
   a.lead = (int *)((char *)a.lb.word + align_up((size_t)tiles * 16, 256));
   GCVL_CK(cudaMemsetAsync(mem, 0, lookback_clear_bytes(tiles), S.stream));
   if (MODE == M_REDUCE) GCVL_CK(cudaMemsetAsync(a.lead, 0xFF, (size_t)tiles * 4, S.stream));
-  k_scan_tma<Op, MODE, SEG><<<tiles, TB_LB, tma_smem<T, MODE>(), S.stream>>>(tin, tout, a);
+  a.wmax = SEG ? wmax_for<T, MODE>(n, m) : 0;
+  k_scan_tma<Op, MODE, SEG><<<tiles, TB_LB, tma_smem<T>(a.wmax), S.stream>>>(tin, tout, a);
   launch_check(name);
   if (MODE == M_REDUCE && tiles > 1) {
     const int chunks = ceil_div(tiles, FIX_NT);
@@ -1170,8 +1177,8 @@ GCVL_EXPORT int gcvl_add_sed_noalloc(vec_p d, vec_p s, vec_p sd, int n, int m) {
     a.lb = lookback_carve(mem, tiles);
     a.status = g_noalloc_status_ptr[dev];
     a.spin_limit = S.spin_limit;
-    if (seg) k_scan_tma<AddD, M_SCAN, true><<<tiles, TB_LB, tma_smem<double, M_SCAN>(), strm>>>(tin, tout, a);
-    else k_scan_tma<AddD, M_SCAN, false><<<tiles, TB_LB, tma_smem<double, M_SCAN>(), strm>>>(tin, tout, a);
+    if (seg) k_scan_tma<AddD, M_SCAN, true><<<tiles, TB_LB, tma_smem<double>(0), strm>>>(tin, tout, a);
+    else k_scan_tma<AddD, M_SCAN, false><<<tiles, TB_LB, tma_smem<double>(0), strm>>>(tin, tout, a);
   } else {
     ScanArgs<double> a;
     a.out = out; a.in = in; a.out2 = nullptr; a.n = n;
