@@ -41,7 +41,13 @@ namespace gcvl {
 constexpr int RK_BLOCK = 256, RK_ITEMS = GCVL_RK_ITEMS, RK_TILE = RK_BLOCK * RK_ITEMS;
 constexpr int RK_WARPS = RK_BLOCK / 32;
 constexpr int RK_MAXPASS = 12;
-constexpr int RK_LB = 32;  // predecessors read per look-back round trip
+#ifndef GCVL_RK_LB
+#define GCVL_RK_LB 4
+#endif
+#ifndef GCVL_RK_MINB
+#define GCVL_RK_MINB 2
+#endif
+constexpr int RK_LB = GCVL_RK_LB;  // predecessors read per look-back round trip
 constexpr int RK_DIRECT_MAX = 1 << 23;
 constexpr int SC_ITEMS = 8;  // elements per thread in the streaming scatter
 constexpr unsigned RK_INC = 0x80000000u;
@@ -147,18 +153,20 @@ __global__ void __launch_bounds__(RK_BLOCK) k_sorted_scatter(V *__restrict__ d, 
                                                              const int *__restrict__ idx, long n,
                                                              const unsigned *__restrict__ gate) {
   if (*(const volatile unsigned *)gate) return;
-  const long i0 = (long)blockIdx.x * (RK_BLOCK * SC_ITEMS) + threadIdx.x;
-  int k[SC_ITEMS];
-  V v[SC_ITEMS];
+  for (long i0 = (long)blockIdx.x * (RK_BLOCK * SC_ITEMS) + threadIdx.x; i0 < n;
+       i0 += (long)gridDim.x * (RK_BLOCK * SC_ITEMS)) {
+    int k[SC_ITEMS];
+    V v[SC_ITEMS];
 #pragma unroll
-  for (int u = 0; u < SC_ITEMS; u++) {
-    const long i = i0 + (long)u * RK_BLOCK;
-    if (i < n) { k[u] = __ldcs(idx + i); v[u] = __ldcs(s + i); }
-  }
+    for (int u = 0; u < SC_ITEMS; u++) {
+      const long i = i0 + (long)u * RK_BLOCK;
+      if (i < n) { k[u] = __ldcs(idx + i); v[u] = __ldcs(s + i); }
+    }
 #pragma unroll
-  for (int u = 0; u < SC_ITEMS; u++) {
-    const long i = i0 + (long)u * RK_BLOCK;
-    if (i < n) d[k[u]] = v[u];
+    for (int u = 0; u < SC_ITEMS; u++) {
+      const long i = i0 + (long)u * RK_BLOCK;
+      if (i < n) d[k[u]] = v[u];
+    }
   }
 }
 
@@ -211,7 +219,7 @@ template <class K, class V, bool AUX, bool STABLE = true> constexpr size_t pass_
 // that only groups pairs by output window (the partitioned scatter) need
 // not: its slots come from shared-memory atomics instead of ballots.
 template <class K, class V, bool AUX, int IN, int OUT, bool STABLE = true>
-__global__ void __launch_bounds__(RK_BLOCK, 2) k_radix_pass(PassArgs<K, V> a) {
+__global__ void __launch_bounds__(RK_BLOCK, GCVL_RK_MINB) k_radix_pass(PassArgs<K, V> a) {
   typedef unsigned short CntT;  // per-warp digit counts (at most 512)
   extern __shared__ __align__(16) unsigned char rk_smem[];
   // staged tile (input order) and the reordered tile
@@ -396,6 +404,9 @@ template <class V>
 __global__ void __launch_bounds__(RK_BLOCK) k_window_scatter(V *__restrict__ d, const unsigned *__restrict__ key,
                                                              const V *__restrict__ val, long n,
                                                              const unsigned *__restrict__ gate) {
+  // one CTA per 2048 pairs, not a grid-stride loop: CTAs dispatched in
+  // order keep the writes within a few windows of the output at a time
+  // (a grid-stride form let the CTAs drift apart: rank 11.6 -> 17.1 ms)
   if (gate && *(const volatile unsigned *)gate == 0) return;
   const long i0 = (long)blockIdx.x * (RK_BLOCK * SC_ITEMS) + threadIdx.x;
   unsigned k[SC_ITEMS];
@@ -426,6 +437,15 @@ void launch_pass(const PassArgs<K, V> &a, int tiles) {
 }
 
 inline int rk_tiles(long n) { return (int)((n + RK_TILE - 1) / RK_TILE); }
+inline int sc_blocks(long n) { return (int)((n + RK_BLOCK * SC_ITEMS - 1) / (RK_BLOCK * SC_ITEMS)); }
+// grid of the sorted-index scatter: grid-stride over at most 16 CTAs per
+// SM, so that when its gate says "not this time" it costs a few
+// microseconds instead of a launch of one CTA per 2048 elements
+inline int sc_grid(long n) {
+  const long need = (n + RK_BLOCK * SC_ITEMS - 1) / (RK_BLOCK * SC_ITEMS);
+  const long cap = (long)st().sm_count * 16;
+  return (int)(need < cap ? (need < 1 ? 1 : need) : cap);
+}
 inline size_t rk_state_bytes(long n) { return (size_t)rk_tiles(n) * 256 * 4; }
 // top-8-bit windows of [0, n)
 inline int window_shift(int n) { int b = bit_length((unsigned)(n > 1 ? n - 1 : 1)); return b > 8 ? b - 8 : 0; }
@@ -475,8 +495,8 @@ void scatter_partitioned(V *d, const V *s, const int *idx, int n, int n_d, vec_p
   // ascending indices (e.g. an interleave): one streaming scatter; otherwise
   // partition by window, then scatter window by window.  The device decides:
   // the kernels of the branch not taken return at once.
-  const long g = ((long)n + RK_BLOCK * SC_ITEMS - 1) / (RK_BLOCK * SC_ITEMS);
-  k_sorted_scatter<V><<<(int)g, RK_BLOCK, 0, S.stream>>>(d, s, idx, n, unsorted);
+  const int g = sc_grid(n);
+  k_sorted_scatter<V><<<g, RK_BLOCK, 0, S.stream>>>(d, s, idx, n, unsorted);
   launch_check("k_sorted_scatter");
   PassArgs<unsigned, V> a{};
   a.kin = (const unsigned *)idx; a.vin = s;
@@ -484,7 +504,7 @@ void scatter_partitioned(V *d, const V *s, const int *idx, int n, int n_d, vec_p
   a.starts = hist; a.state = state; a.counter = counter; a.gate = unsorted;
   a.n = n; a.shift = shift; a.status = S.d_status; a.spin_limit = S.spin_limit;
   launch_pass<unsigned, V, false, IN_ARRAYS, OUT_ARRAYS, false>(a, tiles);
-  k_window_scatter<V><<<(int)g, RK_BLOCK, 0, S.stream>>>(d, a.kout, a.vout, n, unsorted);
+  k_window_scatter<V><<<sc_blocks(n), RK_BLOCK, 0, S.stream>>>(d, a.kout, a.vout, n, unsorted);
   launch_check("k_window_scatter");
 }
 template void scatter_partitioned<unsigned>(unsigned *, const unsigned *, const int *, int, int, vec_p);
@@ -620,8 +640,7 @@ void rank_impl(vec_p d, vec_p s, vec_p sd, int n, int m, vec_p scratch, int is_d
     a.starts = wst; a.state = state; a.counter = counters + RK_MAXPASS;
     a.n = n; a.shift = shift; a.status = S.d_status; a.spin_limit = S.spin_limit;
     launch_pass<unsigned, unsigned, false, IN_ARRAYS, OUT_ARRAYS, false>(a, tiles);
-    const long g = ((long)n + RK_BLOCK * SC_ITEMS - 1) / (RK_BLOCK * SC_ITEMS);
-    k_window_scatter<unsigned><<<(int)g, RK_BLOCK, 0, S.stream>>>((unsigned *)d, iA, (const unsigned *)kA, n,
+    k_window_scatter<unsigned><<<sc_blocks(n), RK_BLOCK, 0, S.stream>>>((unsigned *)d, iA, (const unsigned *)kA, n,
                                                                nullptr);
     launch_check("k_window_scatter");
   }
