@@ -369,24 +369,27 @@ __device__ __forceinline__ void agg_add_split(const double (&x)[ITEMS], unsigned
 // rows: the carry's round trips overlap the load and the fold instead of
 // following them.  The compute warps publish the tile aggregate as soon as it
 // exists and meet the look-back warp only when they need the carry.
-constexpr int TB_LB = TT + 32;  // threads per CTA
+constexpr int TB_LB = TT + 32;  // threads per CTA of a scan
+// A reduction does not wait for earlier tiles, so its CTA has no look-back
+// warp: thread 0 issues the TMA load, and the smaller CTA lets more fit per SM.
+template <int MODE> constexpr int cta_threads() { return MODE == M_REDUCE ? TT : TB_LB; }
 // Resident CTAs per SM the register allocation must allow.  Scans hold no
 // offsets window, so registers, not shared memory, set their occupancy: 8
 // (48-56 registers, a few spilled) measured 4 % faster than 7 on the float64
-// scan and 27 % on the int scan; 9 spills heavily and is slower.  Float64
-// reductions: 7 (their window leaves room for 8 by shared memory, but 8
-// spills).
+// scan and 27 % on the int scan; 9 spills heavily and is slower.
+// Reductions (128-thread CTAs): 8 (float64 reduce 0.90 -> 0.86 ms at 2^28;
+// 9 gains nothing and slows the int reduce).
 #ifndef GCVL_SCAN_MINB
 #define GCVL_SCAN_MINB 8
 #endif
 #ifndef GCVL_RED_MINB_D
-#define GCVL_RED_MINB_D 7
+#define GCVL_RED_MINB_D 8
 #endif
 #ifndef GCVL_RED_MINB_Z
-#define GCVL_RED_MINB_Z 7
+#define GCVL_RED_MINB_Z 8
 #endif
 template <class Op, int MODE, bool SEG>
-__global__ void __launch_bounds__(TB_LB, MODE == M_REDUCE ? (sizeof(typename Op::T) == 8 ? GCVL_RED_MINB_D : GCVL_RED_MINB_Z) : GCVL_SCAN_MINB) k_scan_tma(const __grid_constant__ CUtensorMap tin,
+__global__ void __launch_bounds__(cta_threads<MODE>(), MODE == M_REDUCE ? (sizeof(typename Op::T) == 8 ? GCVL_RED_MINB_D : GCVL_RED_MINB_Z) : GCVL_SCAN_MINB) k_scan_tma(const __grid_constant__ CUtensorMap tin,
                                                      const __grid_constant__ CUtensorMap tout,
                                                      TArgs<typename Op::T> a) {
   typedef typename Op::T T;
@@ -407,15 +410,16 @@ __global__ void __launch_bounds__(TB_LB, MODE == M_REDUCE ? (sizeof(typename Op:
   const int tile = blockIdx.x;
   const long base = (long)tile * TILE;
   const int valid = (int)min((long)TILE, (long)a.n - base);
-  if (tid == TT) {
+  if (tid == (MODE == M_REDUCE ? 0 : TT)) {
     mbar_init(&bar, 1);
     fence_mbar_init();
     mbar_arrive_expect_tx(&bar, TILE * (unsigned)sizeof(T));
     tma_load_2d(tile_b, &tin, &bar, 0, tile * TT);
+    if (MODE == M_REDUCE) s_prefix = Op::ident();
   }
   __syncthreads();  // barrier initialised
 
-  if (warp == NW) {
+  if (MODE != M_REDUCE && warp == NW) {
     // ------------------------------------------------------ look-back warp
     // (reductions do not wait: the one result per tile that needs earlier
     // tiles' part is completed afterwards by k_tile_fix)
@@ -541,7 +545,7 @@ __global__ void __launch_bounds__(TB_LB, MODE == M_REDUCE ? (sizeof(typename Op:
       s_av = av;
     }
   }
-  named_sync(1, TB_LB);  // meet the look-back warp: carry and aggregate exchanged
+  named_sync(1, cta_threads<MODE>());  // meet the look-back warp: carry and aggregate exchanged
   // this thread's exclusive prefix: (earlier tiles) . (earlier warps) . (earlier lanes)
   int pf = s_wpf[warp];
   T pv = s_wpv[warp];
@@ -766,7 +770,7 @@ bool run_scan_tma(typename Op::T *out, const typename Op::T *in, vec_p sd, int n
   GCVL_CK(cudaMemsetAsync(mem, 0, lookback_clear_bytes(tiles), S.stream));
   if (MODE == M_REDUCE) GCVL_CK(cudaMemsetAsync(a.lead, 0xFF, (size_t)tiles * 4, S.stream));
   a.wmax = SEG ? wmax_for<T, MODE>(n, m) : 0;
-  k_scan_tma<Op, MODE, SEG><<<tiles, TB_LB, tma_smem<T>(a.wmax), S.stream>>>(tin, tout, a);
+  k_scan_tma<Op, MODE, SEG><<<tiles, cta_threads<MODE>(), tma_smem<T>(a.wmax), S.stream>>>(tin, tout, a);
   launch_check(name);
   if (MODE == M_REDUCE && tiles > 1) {
     const int chunks = ceil_div(tiles, FIX_NT);
