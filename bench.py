@@ -238,12 +238,12 @@ def primitive_suite(g, n, hbm):
     t = timed(g, lambda: c.rku_luz(dz, xi, n, scr), reps=3)
     # declared pass traffic of this design above 2^23 elements: histograms 4,
     # first pass 4 + 8, two middle passes 16 each, last pass 8 + 8 (index,
-    # position pairs), window partition 8 + 8, window scatter 8 + 4
-    io, passes = 8.0, 92.0
+    # position pairs written grouped by output window), window scatter 8 + 4
+    io, passes = 8.0, 76.0
     out["rku_luz (rank)"] = {"gelem_s": round(n / (t * 1e-3) / 1e9, 2), "ms": round(t, 4),
                              "achieved_gbs_io_floor": round(io * n / (t * 1e-3) / 1e9, 1),
                              "frac_io_floor": round(io * n / (t * 1e-3) / 1e9 / hbm, 3),
-                             "frac_pass_traffic_92B": round(passes * n / (t * 1e-3) / 1e9 / hbm, 3)}
+                             "frac_pass_traffic_76B": round(passes * n / (t * 1e-3) / 1e9 / hbm, 3)}
     g.check(c)
     for p in (xi, yi, dz, fl, ix, ix_seg, lv, sd, scr, red):
         c.fre_fov(p)

@@ -22,11 +22,12 @@
 // The result is the inverse of the sort permutation: rank[index] = position,
 // a scatter to random places.  Below RK_DIRECT_MAX elements the last pass
 // writes it directly (the rank vector fits in L2, which absorbs the random
-// writes).  Above it the last pass writes (index, position) pairs in sorted
-// order, one more pass partitions them by the top 8 bits of the index --
-// 256 windows of the output -- and a streaming kernel writes each window's
-// ranks while the window sits in L2, so DRAM sees whole sectors instead of a
-// read-modify-write per 4-byte element.  smp_pu* uses the same partition and
+// writes).  Above it the last pass writes each (index, position) pair
+// grouped by the top 8 bits of the index -- 256 windows of the output, each
+// element's slot from a second per-window look-back in the same pass -- and
+// a streaming kernel writes each window's ranks while the window sits in
+// L2, so DRAM sees whole sectors instead of a read-modify-write per 4-byte
+// element.  smp_pu* uses the same window partition (a pass of its own) and
 // window scatter for large vectors.
 #include "gcvl.cuh"
 
@@ -54,7 +55,9 @@ constexpr unsigned RK_INC = 0x80000000u;
 
 // where a pass gets its tile from, and where it puts it
 enum { IN_ARRAYS = 0, IN_SRC = 1 };                    // IN_SRC: caller's keys, value = position
-enum { OUT_ARRAYS = 0, OUT_RANK = 1, OUT_PAIRS = 2 };  // OUT_RANK: rank[v] = pos; OUT_PAIRS: (v, pos)
+// OUT_RANK: rank[v] = pos; OUT_WIN: (v, pos) grouped by the output window of
+// v (the partition of the inverse scatter)
+enum { OUT_ARRAYS = 0, OUT_RANK = 1, OUT_WIN = 3 };
 
 __host__ __device__ inline int bit_length(unsigned x) {
   int b = 0;
@@ -199,10 +202,13 @@ template <class K, class V> struct PassArgs {
   const K *kin; const V *vin; const unsigned *ain;
   K *kout; V *vout; unsigned *aout;
   const void *src; int up;            // IN_SRC: the caller's keys
-  int *rank; const int *segoff;       // OUT_RANK / OUT_PAIRS (segmented: rebase by the key)
-  unsigned *pidx, *ppos;              // OUT_PAIRS
+  int *rank; const int *segoff;       // OUT_RANK / OUT_WIN (segmented: rebase by the key)
+  unsigned *pidx, *ppos;              // OUT_WIN
   const unsigned *starts;             // this pass's digit starts
   unsigned *state;                    // [tiles][256] look-back words
+  const unsigned *wstarts;            // OUT_WIN: first slot of every output window
+  unsigned *wstate;                   // OUT_WIN: [tiles][256] look-back words of the window counts
+  int wshift;                         // OUT_WIN: window of v = v >> wshift
   unsigned *counter;
   const unsigned *gate;               // non-null: the pass runs only if *gate is non-zero
   int n, shift;
@@ -213,6 +219,51 @@ template <class K, class V> struct PassArgs {
 template <class K, class V, bool AUX, bool STABLE = true> constexpr size_t pass_smem() {
   return (size_t)RK_TILE * (2 * sizeof(K) + 2 * sizeof(V) + (AUX ? 8 : 0)) + RK_WARPS * 256 * 2 + 256 * 4 +
          256 * 8;
+}
+
+// Publish this tile's count of one bin (digit or window), then look back for
+// the earlier tiles' total.  One 32-bit word per (tile, bin): 0 = not yet,
+// 1 + count = this tile's count (aggregate), RK_INC | prefix = the bin's
+// count in this and all earlier tiles (inclusive; < 2^31 because n is an
+// int).  RK_LB predecessors per round trip, nearest first, until an
+// inclusive count is found (bounded waits).  Each word is self-contained, so
+// relaxed loads suffice and all RK_LB are in flight together; a warp's loads
+// of one predecessor are one 128-byte line.
+__device__ __forceinline__ unsigned bin_lookback(unsigned *state, int tile, int bin, unsigned tot,
+                                                 unsigned *status, int spin_limit) {
+  unsigned *stw = state + (long)tile * 256 + bin;
+  if (tile == 0) {
+    asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(stw), "r"(RK_INC | tot) : "memory");
+    return 0;
+  }
+  asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(stw), "r"(1u + tot) : "memory");
+  unsigned prefix = 0;
+  long t0 = tile - 1;
+  bool done = false;
+  while (!done && t0 >= 0) {
+    unsigned w[RK_LB];
+#pragma unroll
+    for (int j = 0; j < RK_LB; j++) {
+      w[j] = RK_INC;  // beyond tile 0: an inclusive zero
+      if (t0 - j >= 0)
+        asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(w[j]) : "l"(state + (t0 - j) * 256 + bin) : "memory");
+    }
+#pragma unroll
+    for (int j = 0; j < RK_LB; j++) {
+      if (done) break;
+      int it = 0;
+      while (w[j] == 0) {
+        if (++it >= spin_limit) { atomicOr(status, DEV_TIMEOUT); w[j] = RK_INC; break; }
+        __nanosleep(32);
+        asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(w[j]) : "l"(state + (t0 - j) * 256 + bin) : "memory");
+      }
+      if (w[j] & RK_INC) { prefix += w[j] & ~RK_INC; done = true; }
+      else prefix += w[j] - 1u;
+    }
+    t0 -= RK_LB;
+  }
+  asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(stw), "r"(RK_INC | (prefix + tot)) : "memory");
+  return prefix;
 }
 
 // STABLE: equal digits keep their order (every pass of a rank).  A pass
@@ -301,48 +352,7 @@ __global__ void __launch_bounds__(RK_BLOCK, GCVL_RK_MINB) k_radix_pass(PassArgs<
     s_cnt[w * 256 + dd] = (CntT)tot;
     tot += c;
   }
-  // publish this tile's digit count, then look back for earlier tiles'.
-  // One 32-bit word per (tile, digit): 0 = not yet, 1 + count = this tile's
-  // count (aggregate), RK_INC | prefix = count of this digit in this and all
-  // earlier tiles (inclusive; < 2^31 because n is an int).
-  unsigned *stw = a.state + (long)tile * 256 + dd;
-  if (tile == 0) {
-    asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(stw), "r"(RK_INC | tot) : "memory");
-  } else {
-    asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(stw), "r"(1u + tot) : "memory");
-  }
-  // look back for this digit: RK_LB predecessors per round trip, nearest
-  // first, until an inclusive count is found (bounded waits).  Each word is
-  // self-contained, so relaxed loads suffice and all RK_LB are in flight
-  // together; a warp's loads of one predecessor are one 128-byte line.
-  unsigned prefix = 0;
-  if (tile > 0) {
-    long t0 = tile - 1;
-    bool done = false;
-    while (!done && t0 >= 0) {
-      unsigned w[RK_LB];
-#pragma unroll
-      for (int j = 0; j < RK_LB; j++) {
-        w[j] = RK_INC;  // beyond tile 0: an inclusive zero
-        if (t0 - j >= 0)
-          asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(w[j]) : "l"(a.state + (t0 - j) * 256 + dd) : "memory");
-      }
-#pragma unroll
-      for (int j = 0; j < RK_LB; j++) {
-        if (done) break;
-        int it = 0;
-        while (w[j] == 0) {
-          if (++it >= a.spin_limit) { atomicOr(a.status, DEV_TIMEOUT); w[j] = RK_INC; break; }
-          __nanosleep(32);
-          asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(w[j]) : "l"(a.state + (t0 - j) * 256 + dd) : "memory");
-        }
-        if (w[j] & RK_INC) { prefix += w[j] & ~RK_INC; done = true; }
-        else prefix += w[j] - 1u;
-      }
-      t0 -= RK_LB;
-    }
-    asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(stw), "r"(RK_INC | (prefix + tot)) : "memory");
-  }
+  const unsigned prefix = bin_lookback(a.state, tile, dd, tot, a.status, a.spin_limit);
   // exclusive scan of tile counts over the digits -> tile offsets
   {
     unsigned incl = tot;
@@ -361,6 +371,78 @@ __global__ void __launch_bounds__(RK_BLOCK, GCVL_RK_MINB) k_radix_pass(PassArgs<
     s_gb[dd] = (long long)__ldg(a.starts + dd) + (long long)prefix - (long long)loc;
   }
   __syncthreads();
+  if constexpr (OUT == OUT_WIN) {
+    // (v, pos) straight into the output windows of v: each element's sorted
+    // position from the digit offsets (no reorder by digit), then an
+    // unstable slot in its window, the windows' counts looked back over the
+    // earlier tiles like the digits', and a reorder by window so that each
+    // window's run leaves as one coalesced run
+    unsigned pos[RK_ITEMS];
+#pragma unroll
+    for (int c = 0; c < RK_ITEMS; c++) {
+      const unsigned x = wr[c];
+      pos[c] = 0;
+      if (x != 0xFFFFFFFFu) {
+        const int d = (int)(x & 255u);
+        const int e = wbase + c * 32 + lane;
+        long long g = s_gb[d] + s_loc[d] + s_cnt[warp * 256 + d] + (x >> 8);
+        if (a.segoff) g -= __ldg(a.segoff + (int)s_kin[e]);
+        pos[c] = (unsigned)g;
+      }
+    }
+    __syncthreads();  // s_cnt, s_loc and s_gb are free
+    unsigned *s_wc = (unsigned *)s_cnt;  // [256] window counts
+    s_wc[tid] = 0;
+    __syncthreads();
+#pragma unroll
+    for (int c = 0; c < RK_ITEMS; c++) {
+      const int e = wbase + c * 32 + lane;
+      if (wr[c] != 0xFFFFFFFFu) {
+        const unsigned w = (unsigned)s_vin[e] >> a.wshift;
+        wr[c] = (atomicAdd(s_wc + w, 1u) << 8) | w;
+      }
+    }
+    __syncthreads();
+    const unsigned wtot = s_wc[tid];
+    const unsigned wprefix = bin_lookback(a.wstate, tile, tid, wtot, a.status, a.spin_limit);
+    {
+      unsigned incl = wtot;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        unsigned xx = shfl_up(incl, o);
+        if (lane >= o) incl += xx;
+      }
+      if (lane == 31) s_ws[warp] = incl;
+      __syncthreads();
+      unsigned wp = 0;
+#pragma unroll
+      for (int w = 0; w < RK_WARPS; w++) if (w < warp) wp += s_ws[w];
+      const unsigned wloc = wp + incl - wtot;
+      s_loc[tid] = wloc;
+      s_gb[tid] = (long long)__ldg(a.wstarts + tid) + (long long)wprefix - (long long)wloc;
+    }
+    __syncthreads();
+    unsigned *s_ov = (unsigned *)s_kout;  // v by window slot
+#pragma unroll
+    for (int c = 0; c < RK_ITEMS; c++) {
+      const unsigned x = wr[c];
+      if (x != 0xFFFFFFFFu) {
+        const int e = wbase + c * 32 + lane;
+        const unsigned lp = s_loc[x & 255u] + (x >> 8);
+        s_ov[lp] = (unsigned)s_vin[e];
+        s_vout[lp] = (V)pos[c];
+      }
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int e = tid; e < valid; e += RK_BLOCK) {
+      const unsigned v = s_ov[e];
+      const long g = s_gb[v >> a.wshift] + e;
+      a.pidx[g] = v;
+      a.ppos[g] = (unsigned)s_vout[e];
+    }
+    return;
+  }
   // reorder the tile in shared memory
 #pragma unroll
   for (int c = 0; c < RK_ITEMS; c++) {
@@ -385,15 +467,10 @@ __global__ void __launch_bounds__(RK_BLOCK, GCVL_RK_MINB) k_radix_pass(PassArgs<
       a.kout[g] = k;
       a.vout[g] = s_vout[e];
       if (AUX) a.aout[g] = s_aout[e];
-    } else {
+    } else {  // OUT_RANK
       int r = (int)g;
       if (a.segoff) r -= __ldg(a.segoff + (int)k);
-      if (OUT == OUT_RANK) {
-        a.rank[(unsigned)s_vout[e]] = r;
-      } else {
-        a.pidx[g] = (unsigned)s_vout[e];
-        a.ppos[g] = (unsigned)r;
-      }
+      a.rank[(unsigned)s_vout[e]] = r;
     }
   }
 }
@@ -513,7 +590,7 @@ template void scatter_partitioned<unsigned long long>(unsigned long long *, cons
 
 // ------------------------------------------------------------- rank ---
 struct RankLayout {
-  size_t key_a, key_b, idx_a, idx_b, aux_a, aux_b, hist, state, counter, total;
+  size_t key_a, key_b, idx_a, idx_b, aux_a, aux_b, hist, state, wstate, counter, total;
 };
 inline RankLayout rank_layout(int n, int is_double, int seg) {
   RankLayout L;
@@ -529,6 +606,7 @@ inline RankLayout rank_layout(int n, int is_double, int seg) {
   L.hist = take((RK_MAXPASS + 1) * 256 * 4);  // every pass's digit starts, then the window starts
   L.counter = take((RK_MAXPASS + 1) * 4);
   L.state = take(rk_state_bytes(n));
+  L.wstate = take(n > RK_DIRECT_MAX ? rk_state_bytes(n) : 0);  // the last pass's window look-back
   L.total = o + 256;  // room to align the base
   return L;
 }
@@ -582,8 +660,17 @@ void rank_impl(vec_p d, vec_p s, vec_p sd, int n, int m, vec_p scratch, int is_d
   unsigned *aA = seg ? (unsigned *)(mem + L.aux_a) : nullptr, *aB = seg ? (unsigned *)(mem + L.aux_b) : nullptr;
   const int *segoff = seg ? seg_view(sd, n, m).off : nullptr;
   // last pass output when the ranks go through the window partition: the
-  // pair arrays take the buffers the last pass does not read
+  // pair arrays take the buffers the last pass does not read, grouped by
+  // the window of the index (256 windows of the rank vector)
   unsigned *pidx = nullptr, *ppos = nullptr;
+  const int wshift = window_shift(n);
+  unsigned *wst = hist + RK_MAXPASS * 256;
+  unsigned *wstate = (unsigned *)(mem + L.wstate);
+  if (!direct) {
+    k_window_starts<<<1, 256, 0, S.stream>>>(wst, n, wshift);
+    launch_check("k_window_starts");
+    GCVL_CK(cudaMemsetAsync(wstate, 0, rk_state_bytes(n), S.stream));
+  }
   for (int q = 0; q < passes; q++) {
     GCVL_CK(cudaMemsetAsync(state, 0, rk_state_bytes(n), S.stream));
     const bool final = (q == passes - 1);
@@ -595,6 +682,7 @@ void rank_impl(vec_p d, vec_p s, vec_p sd, int n, int m, vec_p scratch, int is_d
       a.kout = (K *)kB; a.vout = iB; a.aout = aB;
       a.src = s; a.up = up;
       a.rank = (int *)d; a.segoff = nullptr; a.pidx = pidx; a.ppos = ppos;
+      a.wstarts = wst; a.wstate = wstate; a.wshift = wshift;
       a.starts = hist + q * 256; a.state = state; a.counter = counters + q;
       a.n = n; a.shift = 8 * q; a.status = S.d_status; a.spin_limit = S.spin_limit;
       if (seg) {
@@ -606,7 +694,7 @@ void rank_impl(vec_p d, vec_p s, vec_p sd, int n, int m, vec_p scratch, int is_d
       } else if (direct) {
         launch_pass<K, unsigned, false, IN_ARRAYS, OUT_RANK>(a, tiles);
       } else {
-        launch_pass<K, unsigned, false, IN_ARRAYS, OUT_PAIRS>(a, tiles);
+        launch_pass<K, unsigned, false, IN_ARRAYS, OUT_WIN>(a, tiles);
       }
     } else {
       // segment passes: the segment number is the key, indices ride along
@@ -615,11 +703,12 @@ void rank_impl(vec_p d, vec_p s, vec_p sd, int n, int m, vec_p scratch, int is_d
       a.kin = first_seg ? aA : (const unsigned *)kA; a.vin = iA; a.ain = nullptr;
       a.kout = (unsigned *)kB; a.vout = iB; a.aout = nullptr;
       a.rank = (int *)d; a.segoff = segoff; a.pidx = pidx; a.ppos = ppos;
+      a.wstarts = wst; a.wstate = wstate; a.wshift = wshift;
       a.starts = hist + q * 256; a.state = state; a.counter = counters + q;
       a.n = n; a.shift = 8 * (q - key_passes); a.status = S.d_status; a.spin_limit = S.spin_limit;
       if (!final) launch_pass<unsigned, unsigned, false, IN_ARRAYS, OUT_ARRAYS>(a, tiles);
       else if (direct) launch_pass<unsigned, unsigned, false, IN_ARRAYS, OUT_RANK>(a, tiles);
-      else launch_pass<unsigned, unsigned, false, IN_ARRAYS, OUT_PAIRS>(a, tiles);
+      else launch_pass<unsigned, unsigned, false, IN_ARRAYS, OUT_WIN>(a, tiles);
     }
     if (!final) {
       std::swap(kA, kB); std::swap(iA, iB);
@@ -627,20 +716,9 @@ void rank_impl(vec_p d, vec_p s, vec_p sd, int n, int m, vec_p scratch, int is_d
     }
   }
   if (!direct) {
-    // (index, position) pairs in sorted order -> windows of the index ->
+    // (index, position) pairs grouped by window of the index ->
     // rank[index] = position, one window at a time
-    const int shift = window_shift(n);
-    unsigned *wst = hist + RK_MAXPASS * 256;
-    k_window_starts<<<1, 256, 0, S.stream>>>(wst, n, shift);
-    launch_check("k_window_starts");
-    GCVL_CK(cudaMemsetAsync(state, 0, rk_state_bytes(n), S.stream));
-    PassArgs<unsigned, unsigned> a{};
-    a.kin = pidx; a.vin = ppos;
-    a.kout = iA; a.vout = (unsigned *)kA;  // free: the last pass read (kA, iA)
-    a.starts = wst; a.state = state; a.counter = counters + RK_MAXPASS;
-    a.n = n; a.shift = shift; a.status = S.d_status; a.spin_limit = S.spin_limit;
-    launch_pass<unsigned, unsigned, false, IN_ARRAYS, OUT_ARRAYS, false>(a, tiles);
-    k_window_scatter<unsigned><<<sc_blocks(n), RK_BLOCK, 0, S.stream>>>((unsigned *)d, iA, (const unsigned *)kA, n,
+    k_window_scatter<unsigned><<<sc_blocks(n), RK_BLOCK, 0, S.stream>>>((unsigned *)d, pidx, (const unsigned *)ppos, n,
                                                                nullptr);
     launch_check("k_window_scatter");
   }
