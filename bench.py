@@ -188,8 +188,9 @@ def timed(g, fn, reps=5):
     return statistics.median(ts)
 
 
-def primitive_suite(g, n, hbm):
-    """Gelem/s and roofline fraction of the other CVL primitives at n."""
+def primitive_suite(g, n, hbm, only=None):
+    """Gelem/s and roofline fraction of the other CVL primitives at n.
+    only: names to run (a name is an entry's first word, e.g. "rku_luz")."""
     from neslgpu_gb300 import workloads as W
     c = g.c
     out = {}
@@ -216,7 +217,12 @@ def primitive_suite(g, n, hbm):
     ix_seg = g.alloc(c.siz_foz(n))
     c.rku_lez(ix_seg, yi, sd, n, m, scr)
 
+    def wanted(name):
+        return only is None or name.split(" ")[0] in only
+
     def rec(name, fn, bytes_per_elem, extra=0.0):
+        if not wanted(name):
+            return
         t = timed(g, fn)
         gb = (bytes_per_elem * n + extra) / (t * 1e-3) / 1e9
         out[name] = {"gelem_s": round(n / (t * 1e-3) / 1e9, 2), "ms": round(t, 4),
@@ -235,15 +241,16 @@ def primitive_suite(g, n, hbm):
     rec("smp_puz (permute)", lambda: c.smp_puz(dz, xi, ix, n, None), 12)
     rec("bck_puz (back-permute)", lambda: c.bck_puz(dz, xi, ix, n, n, None), 12)
     rec("add_wuz", lambda: c.add_wuz(dz, xi, yi, n, None), 12)
-    t = timed(g, lambda: c.rku_luz(dz, xi, n, scr), reps=3)
+    t = timed(g, lambda: c.rku_luz(dz, xi, n, scr), reps=3) if wanted("rku_luz") else None
     # declared pass traffic of this design above 2^23 elements: histograms 4,
     # first pass 4 + 8, two middle passes 16 each, last pass 8 + 8 (index,
     # position pairs written grouped by output window), window scatter 8 + 4
     io, passes = 8.0, 76.0
-    out["rku_luz (rank)"] = {"gelem_s": round(n / (t * 1e-3) / 1e9, 2), "ms": round(t, 4),
-                             "achieved_gbs_io_floor": round(io * n / (t * 1e-3) / 1e9, 1),
-                             "frac_io_floor": round(io * n / (t * 1e-3) / 1e9 / hbm, 3),
-                             "frac_pass_traffic_76B": round(passes * n / (t * 1e-3) / 1e9 / hbm, 3)}
+    if t is not None:
+        out["rku_luz (rank)"] = {"gelem_s": round(n / (t * 1e-3) / 1e9, 2), "ms": round(t, 4),
+                                 "achieved_gbs_io_floor": round(io * n / (t * 1e-3) / 1e9, 1),
+                                 "frac_io_floor": round(io * n / (t * 1e-3) / 1e9 / hbm, 3),
+                                 "frac_pass_traffic_76B": round(passes * n / (t * 1e-3) / 1e9 / hbm, 3)}
     g.check(c)
     for p in (xi, yi, dz, fl, ix, ix_seg, lv, sd, scr, red):
         c.fre_fov(p)
@@ -780,6 +787,8 @@ def main():
     ap.add_argument("--no-suite", action="store_true")
     ap.add_argument("--suite-only", action="store_true",
                     help="only the per-primitive table at 2^log2n (for profiling)")
+    ap.add_argument("--prims", default=None,
+                    help="with --suite-only: comma-separated primitives to time (e.g. rku_luz,pk2_lez)")
     ap.add_argument("--batched-only", action="store_true", help="only the batched workload")
     ap.add_argument("--dispatch-only", action="store_true", help="only the learned-dispatcher sweep")
     ap.add_argument("--vinterp-only", action="store_true", help="only the VCODE programs")
@@ -792,7 +801,8 @@ def main():
         reference_arm(a)
     elif a.suite_only:
         g = Gpu()
-        print(json.dumps({"primitives": primitive_suite(g, 1 << a.log2n, peaks()[0])}))
+        only = set(a.prims.split(",")) if a.prims else None
+        print(json.dumps({"primitives": primitive_suite(g, 1 << a.log2n, peaks()[0], only)}))
     elif a.batched_only:
         print(json.dumps({"batched": batched_suite(Gpu())}))
     elif a.vinterp_only:
