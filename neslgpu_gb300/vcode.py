@@ -28,7 +28,9 @@ library or, for the parity tests and the CPU baseline, the oracle.
 from __future__ import annotations
 
 import re
+import sys
 import time
+import warnings
 from dataclasses import dataclass
 
 import numpy as np
@@ -232,6 +234,85 @@ class Heap:
         self.free.clear()
 
 
+# ------------------------------------------------------------------ I/O ---
+NULL_STREAM_FD = -1
+MAX_FILES = 64
+_OPEN_CLOSE = {"INT": "()", "FLOAT": "()", "BOOL": "()", "SEGDES": "[]", "CHAR": '""'}
+
+
+def format_vector(kind: str, a) -> str:
+    """A vector as vinterp writes it: "( 1 2 3 )", floats in %.14e, booleans
+    as T/F, a segment descriptor as "[ lengths ]"; one line."""
+    if kind == "F":
+        body = "".join(f" {x:.14e}" for x in a)
+    elif kind == "B":
+        body = "".join(" T" if x else " F" for x in a)
+    else:
+        body = "".join(f" {int(x)}" for x in a)
+    o, c = ("[", "]") if kind == "S" else ("(", ")")
+    return f"{o}{body} {c}\n"
+
+
+class _VStream:
+    """A VCODE file: a text stream read vector by vector."""
+
+    def __init__(self, f):
+        self.f = f
+        self.buf = ""
+
+    def _fill(self) -> bool:
+        chunk = self.f.read(1 << 16)
+        self.buf += chunk
+        return bool(chunk)
+
+    def write(self, text: str):
+        self.f.write(text)
+        self.f.flush()
+
+    def read_vector(self, typ: str):
+        """(values, None) or (None, error message)."""
+        start, end = _OPEN_CLOSE.get(typ, "()")
+        while True:
+            self.buf = self.buf.lstrip()
+            if self.buf or not self._fill():
+                break
+        if not self.buf or self.buf[0] != start:
+            self.buf = self.buf[1:]
+            return None, f"vinterp: input error: vector must start with {start}"
+        self.buf = self.buf[1:]
+        parts = []
+        while True:
+            j = self.buf.find(end)
+            if j >= 0:
+                parts.append(self.buf[:j])
+                self.buf = self.buf[j + 1:]
+                break
+            parts.append(self.buf)
+            self.buf = ""
+            if not self._fill():
+                return None, f"input error: vector must end with {end}"
+        body = "".join(parts)
+        if typ == "CHAR":
+            return np.frombuffer(body.encode("latin-1"), dtype=np.uint8).astype(np.int32), None
+        if typ == "BOOL":
+            flags = body.replace(" ", "").replace("\t", "").replace("\n", "")
+            if flags.strip("TF"):
+                return None, f"input error: vector must end with {end}"
+            return np.frombuffer(flags.encode(), dtype=np.uint8) == ord("T"), None
+        if not body.strip():
+            return np.empty(0, dtype=np.float64 if typ == "FLOAT" else np.int32), None
+        with warnings.catch_warnings():
+            warnings.simplefilter("error")
+            try:
+                if typ == "FLOAT":
+                    return np.fromstring(body, dtype=np.float64, sep=" "), None
+                v = np.fromstring(body, dtype=np.int64, sep=" ")
+            except (ValueError, DeprecationWarning, RuntimeWarning):
+                return None, f"input error: vector must end with {end}"
+        # 32-bit wrap-around, as vinterp's own integer parser
+        return (v & 0xFFFFFFFF).astype(np.uint32).view(np.int32), None
+
+
 # ----------------------------------------------------------- interpreter ---
 class Interpreter:
     """Runs a parsed VCODE program on one CVL implementation."""
@@ -250,6 +331,8 @@ class Interpreter:
         self.timer = 0.0
         self.ops_run = 0
         self._fn = {}
+        # VCODE file descriptors: 0, 1, 2 are the standard streams
+        self.files: dict[int, _VStream] = {0: _VStream(sys.stdin), 1: _VStream(sys.stdout), 2: _VStream(sys.stderr)}
 
     # -- memory
     def fn(self, name):
@@ -614,14 +697,110 @@ class Interpreter:
             s = st[-1]
             self.fn("rnd_foz")(self.scalar_int(s))
             self._finish(1, [self.const_scalar("B", True)])
-        elif op == "WRITE":
-            v = st.pop()
-            print(self.to_host(v))
-            self.drop(v)
-            st.append(self.new("I", 0))
-            st.append(self.const_scalar("B", True))
+        elif op in ("READ", "WRITE", "FREAD", "FWRITE", "FOPEN", "FCLOSE"):
+            self._io(ins)
         else:
             raise VcodeError(f"line {ins.line}: {op} is not supported")
+
+    # -- I/O (vinterp's nesl/vcode/io.c: text forms "(1 2 3)" INT, "(1.0 2.0)"
+    # FLOAT, "(T F)" BOOL, "[1 2 3]" SEGDES by its lengths, "\"text\"" CHAR as
+    # character codes; every operation leaves an error string -- empty on
+    # success -- and a success flag on top of the stack)
+    def _push_io_status(self, err: str | None):
+        codes = np.frombuffer(err.encode("latin-1"), dtype=np.uint8).astype(np.int32) if err else []
+        self.stack.append(self.from_host("I", codes))
+        self.stack.append(self.const_scalar("B", not err))
+
+    def _fd_from_stack(self, ins):
+        v = self.stack.pop()
+        fd = self.scalar_int(v)
+        self.drop(v)
+        if fd == NULL_STREAM_FD:
+            return fd, None  # as vinterp: no message, and no stream
+        if fd not in self.files:
+            return None, f"vinterp: line {ins.line}: illegal VCODE file descriptor for {ins.op}: {fd}"
+        return fd, None
+
+    def _read(self, ins, stream):
+        kind = KIND_OF.get(ins.typ, "I")
+        empty_kind = "I" if kind == "S" or ins.typ == "CHAR" else kind
+        value, err = stream.read_vector(ins.typ) if stream is not None else (None, None)
+        if value is None:
+            self.stack.append(self.new(empty_kind, 0))
+        elif ins.typ == "SEGDES":
+            lens = self.from_host("I", value)
+            self.stack.append(self.segdes_from_lengths(lens))
+            self.drop(lens)
+        else:
+            self.stack.append(self.from_host("I" if ins.typ == "CHAR" else kind, value))
+        self._push_io_status(err)
+
+    def _write(self, ins, stream):
+        v = self.stack.pop()
+        err = None
+        try:
+            if ins.typ == "CHAR":
+                stream.write("".join(map(chr, self.to_host(v).tolist())))
+            else:
+                stream.write(format_vector(v.kind, self.to_host(v)))
+        except (OSError, ValueError) as e:
+            err = str(e)
+        self.drop(v)
+        self._push_io_status(err)
+
+    def _io(self, ins):
+        st = self.stack
+        op = ins.op
+        if op == "READ":
+            self._read(ins, self.files[0])
+        elif op == "WRITE":
+            self._write(ins, self.files[1])
+        elif op == "FREAD":
+            fd, err = self._fd_from_stack(ins)
+            if fd is None or fd < 0:
+                st.append(self.new("I" if ins.typ in ("SEGDES", "CHAR") else KIND_OF.get(ins.typ, "I"), 0))
+                self._push_io_status(err)
+            else:
+                self._read(ins, self.files[fd])
+        elif op == "FWRITE":
+            fd, err = self._fd_from_stack(ins)
+            if fd is None or fd < 0:
+                self.drop(st.pop())
+                self._push_io_status(err or f"illegal VCODE file descriptor in FWRITE")
+            else:
+                self._write(ins, self.files[fd])
+        elif op == "FOPEN":
+            mv = st.pop()
+            mode = self.scalar_int(mv)
+            self.drop(mv)
+            if mode not in (1, 2, 3):
+                raise VcodeError(f"line {ins.line}: FOPEN: top of stack ({mode}) not legal mode.")
+            nv = st.pop()
+            name = "".join(map(chr, self.to_host(nv).tolist()))
+            self.drop(nv)
+            fd, err = -1, None
+            try:
+                f = open(name, {1: "r", 2: "w", 3: "a"}[mode])
+                free = [k for k in range(3, MAX_FILES) if k not in self.files]
+                if free:
+                    fd = free[0]
+                    self.files[fd] = _VStream(f)
+                else:
+                    f.close()
+                    err = "no room in internal file table"
+            except OSError as e:
+                err = e.strerror or str(e)
+            st.append(self.from_host("I", [fd]))
+            self._push_io_status(err)
+        elif op == "FCLOSE":
+            fd, err = self._fd_from_stack(ins)
+            if fd is not None and fd >= 0:
+                stream = self.files.pop(fd)
+                if fd > 2:
+                    stream.f.close()
+                else:
+                    stream.f.flush()
+            self._push_io_status(err)
 
     def _finish(self, nargs, results):
         st = self.stack
