@@ -1001,11 +1001,26 @@ __global__ void k_granules(SegView sv, int *gran, int ng) {
 }
 
 // Head bitmap: one bit per element, set where a non-empty segment starts.
+// Offsets ascend, so the lanes whose segment starts fall in one bitmap word
+// are contiguous: their bits are OR-ed within the warp first and one atomic
+// per run sets them (with one-element segments a word takes 32 heads).
 __global__ void k_headbits(SegView sv, unsigned *bits) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= sv.m) return;
-  const int o = sv.off[s];
-  if (sv.off[s + 1] > o) atomicOr(bits + (o >> 5), 1u << (o & 31));
+  const int lane = threadIdx.x & 31;
+  int word = -1;
+  unsigned bit = 0;
+  if (s < sv.m) {
+    const int o = sv.off[s];
+    if (sv.off[s + 1] > o) { word = o >> 5; bit = 1u << (o & 31); }
+  }
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const int w2 = __shfl_down_sync(0xffffffffu, word, d);
+    const unsigned b2 = __shfl_down_sync(0xffffffffu, bit, d);
+    if (lane + d < 32 && w2 == word) bit |= b2;
+  }
+  const int wprev = __shfl_up_sync(0xffffffffu, word, 1);
+  if (word >= 0 && (lane == 0 || wprev != word)) atomicOr(bits + word, bit);
 }
 
 void make_segdes(vec_p sd, vec_p l, int n, int m, vec_p scratch) {
