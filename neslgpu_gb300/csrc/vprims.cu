@@ -270,28 +270,6 @@ template <class T> struct RepSeg {  // d[off[g] + i[g]] = v[g]
   T *d; const int *i; const T *v; const int *off;
   __device__ void operator()(long g) const { d[(long)off[g] + i[g]] = v[g]; }
 };
-template <class T> struct DisSeg {  // d[k] = v[seg(k)]
-  T *d; const T *v;
-  __device__ void operator()(int k, int s, int) const { d[k] = __ldg(v + s); }
-};
-struct IndSeg {  // d[k] = init[s] + stride[s] * (k - start)
-  int *d; const int *init; const int *stride;
-  __device__ void operator()(int k, int s, int start) const {
-    d[k] = (int)((unsigned)__ldg(init + s) + (unsigned)__ldg(stride + s) * (unsigned)(k - start));
-  }
-};
-template <class T> struct Perm {  // d[i[k]] = s[k]
-  T *d; const T *s; const int *i;
-  __device__ void operator()(long k) const { d[__ldg(i + k)] = __ldcs(s + k); }
-};
-template <class T> struct PermSeg {  // d[start + i[k]] = s[k]
-  T *d; const T *s; const int *i;
-  __device__ void operator()(int k, int, int start) const { d[(long)start + __ldg(i + k)] = __ldcs(s + k); }
-};
-template <class T> struct BPerm {  // d[k] = s[i[k]]
-  T *d; const T *s; const int *i;
-  __device__ void operator()(long k) const { d[k] = __ldg(s + __ldg(i + k)); }
-};
 template <class T> struct BPermSeg {  // d[k] = s[off_s[seg_d(k)] + i[k]]
   T *d; const T *s; const int *i; const int *off_s; int m_s;
   __device__ void operator()(int k, int sg, int) const {
