@@ -504,8 +504,46 @@ __global__ void __launch_bounds__(cta_threads<MODE>(), MODE == M_REDUCE ? (sizeo
 
   int tf;
   T tv;
-  if constexpr (MODE == M_REDUCE && std::is_same<Op, AddD>::value) agg_add_split<ITEMS>(x, heads, cnt, tf, tv);
-  else Engine<Op, ITEMS>::agg(x, heads, cnt, tf, tv);
+  // Reductions other than float64 + take one pass over the thread's items:
+  // the results of segments that start and end among them are final at
+  // once; the first segment end, whose segment began before these items,
+  // waits for the earlier threads' prefix (first_s, first_v).  Float64 +
+  // folds in fixed point per piece below.
+  constexpr bool ONE_PASS = SEG && MODE == M_REDUCE && !std::is_same<Op, AddD>::value;
+  int first_s = -1;
+  T first_v = Op::ident();
+  if constexpr (ONE_PASS) {
+    T r = Op::ident();
+    bool started = false;
+    if (cnt > 0) {
+      const int m = a.sv.m;
+      if (k0 == 0)
+        for (int q = 0; q < s0; q++) a.out[q] = Op::init();  // empty segments before element 0
+      int sg = s0;
+      int end = off(sg + 1);
+#pragma unroll
+      for (int i = 0; i < ITEMS; i++) {
+        if (i < cnt) {
+          if ((heads >> i) & 1u) { r = Op::init(); started = true; }
+          r = Op::apply(r, x[i]);
+          if (k0 + i + 1 == end) {
+            if (started) a.out[sg] = r;
+            else { first_s = sg; first_v = r; }
+            int s2 = sg + 1;
+            while (s2 < m && off(s2 + 1) == end) { a.out[s2] = Op::init(); ++s2; }
+            sg = s2;
+            if (sg < m) end = off(sg + 1);
+          }
+        }
+      }
+    }
+    tf = heads != 0;
+    tv = r;
+  } else if constexpr (MODE == M_REDUCE && std::is_same<Op, AddD>::value) {
+    agg_add_split<ITEMS>(x, heads, cnt, tf, tv);
+  } else {
+    Engine<Op, ITEMS>::agg(x, heads, cnt, tf, tv);
+  }
 
   // warp inclusive scan of (head, value)
   int f = tf;
@@ -579,6 +617,11 @@ __global__ void __launch_bounds__(cta_threads<MODE>(), MODE == M_REDUCE ? (sizeo
       tma_store_2d(&tout, tile_b, 0, tile * TT);
       bulk_commit();
       bulk_wait_read_all();
+    }
+  } else if constexpr (ONE_PASS) {  // the one result still lacking the earlier part
+    if (first_s >= 0) {
+      a.out[first_s] = Op::apply(run, first_v);
+      if (!pf) a.lead[tile] = first_s;  // began in an earlier tile
     }
   } else {  // M_REDUCE: results at segment ends
     if (cnt > 0) {
