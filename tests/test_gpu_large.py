@@ -130,7 +130,7 @@ def test_segmented_permute_many_segments(gpu, oracle, data, t):
     compare("exact", ops.smp_e(gpu, f"smp_pe{t}", x, idx, lens), ops.smp_e(oracle, f"smp_pe{t}", x, idx, lens))
 
 
-@pytest.mark.parametrize("mean", [1.0, 1.7, 2.5])
+@pytest.mark.parametrize("mean", [1.0, 1.7, 2.5, 3.5])
 def test_reductions_tiny_segments(gpu, oracle, mean):
     """Segmented reductions whose tiles hold as many segments as elements
     (the shared-memory offsets window) or more (empty segments: global
@@ -145,3 +145,13 @@ def test_reductions_tiny_segments(gpu, oracle, mean):
         compare("exact", ops.reduce_e(gpu, name, x, lens), ops.reduce_e(oracle, name, x, lens))
     compare("sum", ops.reduce_e(gpu, "add_red", xd, lens), ops.reduce_e(oracle, "add_red", xd, lens),
             seg_abs_total(xd, lens))
+
+
+@pytest.mark.parametrize("n", [64 * 4096 - 1, 64 * 4096, 64 * 4096 + 1, 1 << 22])
+def test_pack_two_pass_edges(gpu, oracle, n):
+    """Around the size where pack switches to two passes (64 tiles of 4096),
+    with all-false, all-true and alternating flags."""
+    r = W.rng(n % 1000)
+    x = r.integers(-2 ** 31, 2 ** 31, size=n, dtype=np.int64).astype(np.int32)
+    for fl in (np.zeros(n, np.int32), np.ones(n, np.int32), (np.arange(n) % 2).astype(np.int32)):
+        compare("exact", ops.pack_u(gpu, "pk2_luz", x, fl), ops.pack_u(oracle, "pk2_luz", x, fl))
