@@ -83,13 +83,15 @@ __device__ __forceinline__ int swz(int r, int c) { return r * 128 + (((c ^ r) & 
 
 // ------------------------------------------- float64 sums in integers ---
 // A thread's group of at most 16 doubles is summed in 64-bit fixed point at
-// the scale of its largest exponent `emax`: each value is rounded to a
-// multiple of 2^(emax-1075) -- the unit in the last place of the largest
-// value -- and the integers are added exactly (sixteen 53-bit mantissas fit
-// in 57 bits); the total is converted to double once.  The error is at most
-// 8 ulp of the group's largest value, of the order of a sequential float64
-// sum's own rounding, and the work runs on the integer pipes instead of the
-// GB300's narrow FP64 pipe (2 FP64 operations per clock per SM).
+// the scale of its largest exponent `emax`: each value's magnitude is
+// truncated to a multiple of 2^(emax-1075) -- the unit in the last place of
+// the largest value -- and the integers are added exactly (sixteen 53-bit
+// mantissas fit in 57 bits); the total is converted to double once.  The
+// error is under 16 ulp of the group's largest value, so over a segment
+// under 2^-48 of the sum of the magnitudes, and the work runs on the integer
+// pipes instead of GB300's narrow FP64 pipe (2 FP64 operations per clock per
+// SM).  Truncating instead of rounding each addend measured 6 % faster on
+// the float64 reduction.
 __device__ __forceinline__ int fx_exp(unsigned long long b) {
   int e = (int)((b >> 52) & 0x7FF);
   return e ? e : 1;
@@ -99,7 +101,7 @@ __device__ __forceinline__ void fx_add(long long &acc, unsigned long long b, int
   unsigned long long m = b & 0xFFFFFFFFFFFFFULL;
   if (e) m |= 1ULL << 52; else e = 1;
   const int d = min(emax - e, 63);
-  const unsigned long long v = (m + ((1ULL << d) >> 1)) >> d;
+  const unsigned long long v = m >> d;  // magnitude truncated to the common scale
   const long long sgn = (long long)b >> 63;  // 0 or -1
   acc += ((long long)v ^ sgn) - sgn;
 }
