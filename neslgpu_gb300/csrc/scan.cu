@@ -335,7 +335,7 @@ template <int ITEMS> struct Engine<AddD, ITEMS> {
 #pragma unroll
     for (int i = 0; i < ITEMS; i++)
       if (i >= from && i < cnt) fx_add(acc, (unsigned long long)__double_as_longlong(x[i]), emax);
-    tv = fx_to_double(acc, emax);  // never -0.0, so starting from init 0.0 changes nothing
+    tv = fx_to_double_alu(acc, emax);  // never -0.0, so starting from init 0.0 changes nothing
   }
 };
 
