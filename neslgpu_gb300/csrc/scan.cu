@@ -631,10 +631,17 @@ __global__ void __launch_bounds__(cta_threads<MODE>(), MODE == M_REDUCE ? (sizeo
       int s = s0;
       int end = off(s + 1);
       if constexpr (std::is_same<Op, AddD>::value) {
-        // pieces between heads, each summed in fixed point
+        // pieces between heads, each summed in fixed point.  Element i ends
+        // a non-empty segment exactly when element i+1 is a head (or past
+        // the end): only those positions are visited (mostly none).
+        const int kn = k0 + cnt;
+        const unsigned nh = kn >= a.n ? 1u : (__ldg(a.sv.bits + (kn >> 5)) >> (kn & 31)) & 1u;
+        unsigned ends = ((heads >> 1) | (nh << (cnt - 1))) & (cnt >= 32 ? ~0u : ((1u << cnt) - 1u));
         int ps = 0;
-        for (int i = 0; i < cnt; i++) {
-          if (k0 + i + 1 == end) {
+        while (ends) {
+          const int i = __ffs(ends) - 1;
+          ends &= ends - 1;
+          {
             double pv2 = fx_range<ITEMS>(x, ps, i + 1);
             a.out[s] = ((heads >> ps) & 1u) ? pv2 : AddD::apply(run, pv2);
             if (!pf && !(heads & ((2u << i) - 1u))) a.lead[tile] = s;  // began in an earlier tile
