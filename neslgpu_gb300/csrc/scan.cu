@@ -341,11 +341,11 @@ template <int ITEMS> struct Engine<AddD, ITEMS> {
 
 // Reductions: a thread's float64 + fold split between the integer pipes
 // (the first GCVL_RED_FX_ITEMS items, fixed point) and the FP64 pipe (the
-// rest, an add chain), so that neither carries the whole fold; 12 of 16
-// measured best (2 % over 8 of 16).  The segmented reduction has no
-// per-element output work to keep the FP64 pipe busy.
+// rest, an add chain), so that neither carries the whole fold; 14 of 16
+// measured best (8 of 16: 16 % slower, 16 of 16: 3 %).  The segmented
+// reduction has no per-element output work to keep the FP64 pipe busy.
 #ifndef GCVL_RED_FX_ITEMS
-#define GCVL_RED_FX_ITEMS 12
+#define GCVL_RED_FX_ITEMS 14
 #endif
 template <int ITEMS>
 __device__ __forceinline__ void agg_add_split(const double (&x)[ITEMS], unsigned heads, int cnt, int &tf,
