@@ -369,6 +369,11 @@ __global__ void __launch_bounds__(RK_BLOCK, GCVL_RK_MINB) k_radix_pass(PassArgs<
     const unsigned loc = wp + incl - tot;
     s_loc[dd] = loc;
     s_gb[dd] = (long long)__ldg(a.starts + dd) + (long long)prefix - (long long)loc;
+    // each warp's counter of this digit becomes the digit's slot in the
+    // reordered tile for that warp (one shared-memory lookup per element
+    // below instead of two; below 4096, so it fits the 16-bit counter)
+#pragma unroll
+    for (int w = 0; w < RK_WARPS; w++) s_cnt[w * 256 + dd] = (CntT)(s_cnt[w * 256 + dd] + loc);
   }
   __syncthreads();
   if constexpr (OUT == OUT_WIN) {
@@ -385,7 +390,7 @@ __global__ void __launch_bounds__(RK_BLOCK, GCVL_RK_MINB) k_radix_pass(PassArgs<
       if (x != 0xFFFFFFFFu) {
         const int d = (int)(x & 255u);
         const int e = wbase + c * 32 + lane;
-        long long g = s_gb[d] + s_loc[d] + s_cnt[warp * 256 + d] + (x >> 8);
+        long long g = s_gb[d] + s_cnt[warp * 256 + d] + (x >> 8);
         if (a.segoff) g -= __ldg(a.segoff + (int)s_kin[e]);
         pos[c] = (unsigned)g;
       }
@@ -449,7 +454,7 @@ __global__ void __launch_bounds__(RK_BLOCK, GCVL_RK_MINB) k_radix_pass(PassArgs<
     const unsigned x = wr[c];
     if (x != 0xFFFFFFFFu) {
       const int d = (int)(x & 255u);
-      const unsigned lp = s_loc[d] + s_cnt[warp * 256 + d] + (x >> 8);
+      const unsigned lp = s_cnt[warp * 256 + d] + (x >> 8);
       const int e = wbase + c * 32 + lane;
       s_kout[lp] = s_kin[e];
       s_vout[lp] = s_vin[e];
