@@ -40,7 +40,11 @@ def test_host_side_functions_without_gpu():
     """Size, scratch, in-place and pointer arithmetic need no device."""
     from neslgpu_gb300.cvl import load
     c = load()
-    assert c.siz_foz(3) == 2 and c.siz_fob(3) == 2 and c.siz_fod(3) == 3
+    # 8-byte units, rounded to even: vinterp's heap then keeps vectors 16-byte aligned
+    assert c.siz_foz(3) == 2 and c.siz_fob(3) == 2 and c.siz_fod(3) == 4 and c.siz_fod(4) == 4
+    assert c.siz_foz(1) == 2 and c.siz_fod(0) == 0
+    assert all(c.siz_foz(k) % 2 == 0 and c.siz_fod(k) % 2 == 0 and c.siz_fos(k, k // 3) % 2 == 0
+               for k in range(0, 200, 7))
     assert c.siz_fos(100, 10) >= c.siz_foz(10)
     assert c.add_fov(1000, 3) == 1024 and c.sub_fov(1024, 1000) == 3
     assert c.cmp_fov(1000, 1024) == -3 and c.eql_fov(8, 8) == 1
