@@ -36,6 +36,7 @@ template <class T> struct ScanArgs {
   int count_flags;   // pk1_lev: fold (x != 0) instead of x
   const int *gidx;   // gather-multiply form: element k is in[k] * gsrc[gidx[k]]
   const T *gsrc;
+  int *lead;         // reductions: per tile, the result lacking the earlier tiles' part (-1: none)
 };
 
 // Coalesced load of a tile into per-thread blocked registers through padded
@@ -188,14 +189,15 @@ k_scan(ScanArgs<typename Op::T> a) {
   pv = ef ? ev : Op::apply(pv, ev);
   pf |= ef;
 
-  // publish and look back
+  // publish and look back (reductions do not wait: the one result per tile
+  // that lacks the earlier tiles' part is completed by k_tile_fix)
   if (warp == 0) {
     // thread 0 holds element `base`: its head bit says whether the tile
     // starts a segment (then no carry from earlier tiles is needed)
     const bool first_head = shfl_idx((int)(heads & 1u), 0) != 0;
     if (lane == 0) lb_publish(a.lb.word + tile, (tile == 0 || af) ? TS_INC : TS_AGG, to_bits<T>(av));
     T P = Op::ident();
-    if (tile > 0 && !first_head) {
+    if (MODE != M_REDUCE && tile > 0 && !first_head) {
       P = lookback_prefix<Op>(a.lb.word, tile, a.status, a.spin_limit);
       if (lane == 0 && !af) lb_publish(a.lb.word + tile, TS_INC, to_bits<T>(Op::apply(P, av)));
     }
@@ -232,6 +234,7 @@ k_scan(ScanArgs<typename Op::T> a) {
         run = Op::apply(run, x[i]);
         if (k0 + i + 1 == end) {
           a.out[s] = run;
+          if (!pf && !(heads & ((2u << i) - 1u))) a.lead[tile] = s;  // began in an earlier tile
           int s2 = s + 1;
           while (s2 < m && __ldg(a.sv.off + s2 + 1) == end) { a.out[s2] = Op::init(); ++s2; }
           s = s2;
@@ -790,6 +793,19 @@ inline size_t reduce_pass_bytes(int tiles) {
   const int chunks = (tiles + 1023) / 1024;
   return lookback_bytes(tiles) + align_up((size_t)tiles * 4, 256) + lookback_bytes(chunks);
 }
+// The fix-up pass of a segmented reduction whose first pass published its
+// tile aggregates at `w` and the per-tile results to complete at `lead`
+// (lead sits right after the look-back area, the chunks' look-back after it).
+template <class Op>
+void launch_tile_fix(const ulonglong2 *w, const int *lead, int tiles, typename Op::T *out) {
+  if (tiles <= 1) return;
+  State &S = st();
+  const int chunks = ceil_div(tiles, FIX_NT);
+  LookbackMem cl = lookback_carve((char *)lead + align_up((size_t)tiles * 4, 256), chunks);
+  GCVL_CK(cudaMemsetAsync(cl.counter, 0, 256 + (size_t)chunks * 16, S.stream));
+  k_tile_fix<Op><<<chunks, FIX_NT, 0, S.stream>>>(w, lead, tiles, out, cl.word, S.d_status, S.spin_limit);
+  launch_check("k_tile_fix");
+}
 template <class T> constexpr size_t tma_smem(int wmax) {
   return 1024 + (size_t)TT * row_items<T>() * sizeof(T) + (size_t)(wmax > 0 ? wpad(wmax) + 1 : 0) * 4;
 }
@@ -822,14 +838,7 @@ bool run_scan_tma(typename Op::T *out, const typename Op::T *in, vec_p sd, int n
   a.wmax = SEG ? wmax_for<T, MODE>(n, m) : 0;
   k_scan_tma<Op, MODE, SEG><<<tiles, cta_threads<MODE>(), tma_smem<T>(a.wmax), S.stream>>>(tin, tout, a);
   launch_check(name);
-  if (MODE == M_REDUCE && tiles > 1) {
-    const int chunks = ceil_div(tiles, FIX_NT);
-    LookbackMem cl = lookback_carve((char *)a.lead + align_up((size_t)tiles * 4, 256), chunks);
-    GCVL_CK(cudaMemsetAsync(cl.counter, 0, 256 + (size_t)chunks * 16, S.stream));
-    k_tile_fix<Op><<<chunks, FIX_NT, 0, S.stream>>>(a.lb.word, a.lead, tiles, out, cl.word, S.d_status,
-                                                   S.spin_limit);
-    launch_check("k_tile_fix");
-  }
+  if (MODE == M_REDUCE) launch_tile_fix<Op>(a.lb.word, a.lead, tiles, out);
   return true;
 }
 
@@ -859,18 +868,21 @@ void run_scan(typename Op::T *out, const typename Op::T *in, typename Op::T *out
     if (tma_ok && run_scan_tma<Op, MODE, SEG>(out, in, sd, n, m, scratch, name)) return;
   }
   const int tiles = ceil_div(n, tile_elems<T>());
-  void *mem = scratch_or_work(scratch, lookback_bytes(tiles));
+  void *mem = scratch_or_work(scratch, MODE == M_REDUCE ? reduce_pass_bytes(tiles) : lookback_bytes(tiles));
   if (!mem) return;
-  ScanArgs<T> a;
+  ScanArgs<T> a{};
   a.out = out; a.in = in; a.out2 = out2; a.n = n;
   a.sv = SEG ? seg_view(sd, n, m) : SegView{nullptr, nullptr, nullptr, nullptr, n, 1};
   a.lb = lookback_carve(mem, tiles);
   a.status = S.d_status;
   a.spin_limit = S.spin_limit;
   a.count_flags = count_flags ? 1 : 0;
+  a.lead = (int *)((char *)a.lb.word + align_up((size_t)tiles * 16, 256));
   GCVL_CK(cudaMemsetAsync(mem, 0, lookback_clear_bytes(tiles), S.stream));
+  if (MODE == M_REDUCE) GCVL_CK(cudaMemsetAsync(a.lead, 0xFF, (size_t)tiles * 4, S.stream));
   k_scan<Op, MODE, SEG><<<tiles, Tiling<T>::BLOCK, 0, S.stream>>>(a);
   launch_check(name);
+  if (MODE == M_REDUCE) launch_tile_fix<Op>(a.lb.word, a.lead, tiles, out);
 }
 
 // Segmented sums of gathered products, y[r] = sum over row r of
@@ -886,7 +898,7 @@ static void run_gather_mul_reduce(double *y, const double *vals, const int *cols
     return;
   }
   const int tiles = ceil_div(nnz, tile_elems<double>());
-  void *mem = scratch_or_work(scratch, lookback_bytes(tiles));
+  void *mem = scratch_or_work(scratch, reduce_pass_bytes(tiles));
   if (!mem) return;
   ScanArgs<double> a{};
   a.out = y; a.in = vals; a.out2 = nullptr; a.n = nnz;
@@ -896,9 +908,12 @@ static void run_gather_mul_reduce(double *y, const double *vals, const int *cols
   a.spin_limit = S.spin_limit;
   a.count_flags = 0;
   a.gidx = cols; a.gsrc = x;
+  a.lead = (int *)((char *)a.lb.word + align_up((size_t)tiles * 16, 256));
   GCVL_CK(cudaMemsetAsync(mem, 0, lookback_clear_bytes(tiles), S.stream));
+  GCVL_CK(cudaMemsetAsync(a.lead, 0xFF, (size_t)tiles * 4, S.stream));
   k_scan<AddD, M_REDUCE, true, true><<<tiles, Tiling<double>::BLOCK, 0, S.stream>>>(a);
   launch_check("gcvl_spmv_csr");
+  launch_tile_fix<AddD>(a.lb.word, a.lead, tiles, y);
 }
 
 // ---------------------------------------------- unsegmented reductions ---
@@ -1286,5 +1301,5 @@ GCVL_EXPORT void gcvl_spmv_csr(vec_p y, vec_p vals, vec_p cols, vec_p x, vec_p s
 }
 GCVL_EXPORT int gcvl_spmv_csr_scratch(int nnz, int rows) {
   (void)rows;
-  return lookback_units(ceil_div(nnz > 0 ? nnz : 1, tile_elems<double>()));
+  return (int)((reduce_pass_bytes(ceil_div(nnz > 0 ? nnz : 1, tile_elems<double>())) + 7) / 8);
 }

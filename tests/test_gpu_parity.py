@@ -53,6 +53,19 @@ def test_parity_unaligned_vectors(oracle, kind):
     _run_all(DeviceRunner(load(), offset=1), oracle, 70_001, kind, seed=21)
 
 
+@pytest.mark.parametrize("kind", ["long", "tiny"])
+def test_parity_unaligned_two_million(oracle, kind):
+    """The non-TMA paths past 2^21 elements: segmented reductions there
+    complete the results that span tiles in a second pass over more than
+    one chunk of tile aggregates."""
+    from neslgpu_gb300.cvl import load
+    from neslgpu_gb300.ops import DeviceRunner
+    from conftest import _has_gpu
+    if not _has_gpu():
+        pytest.skip("no GPU")
+    _run_all(DeviceRunner(load(), offset=1), oracle, (1 << 22) + 13, kind, seed=41)
+
+
 @pytest.mark.parametrize("kind", ["long", "tiny", "empty", "one"])
 def test_parity_two_million(gpu, oracle, kind):
     """Every primitive past 2^21 elements (a thousand tiles and more):
