@@ -676,6 +676,257 @@ __global__ void __launch_bounds__(cta_threads<MODE>(), MODE == M_REDUCE ? (sizeo
   }
 }
 
+// ============================================================================
+// Persistent ring scan: the segmented and unsegmented scans of 16-byte
+// aligned vectors.
+//
+// A CTA runs rounds.  Round r folds the tile loaded for it (one 128-byte row
+// per compute thread) and publishes the tile aggregate, then writes the
+// outputs of the tile it folded in round r-1.  The carry into that older tile
+// depends on tiles folded a round earlier than the fold just done, so the
+// look-back warp collects it while the compute warps fold; a tile-per-CTA
+// scan instead waits, at every tile, for neighbours folded at the same time
+// as itself (35 % of the float64 scan's time at 2^28).  Tiles come from a
+// ticket counter in increasing order and the TMA loads run RING_NB rounds
+// ahead in a ring of tile buffers.  Every tile below a ticket already belongs
+// to a running CTA that folds it without waiting on anything but its own
+// load, so the look-back ends however many CTAs are resident.
+// ============================================================================
+#ifndef GCVL_RING_NB
+#define GCVL_RING_NB 2
+#endif
+#ifndef GCVL_RING_MINB
+#define GCVL_RING_MINB 6
+#endif
+constexpr int RING_NB = GCVL_RING_NB;
+template <class T> constexpr size_t ring_smem() { return 1024 + (size_t)RING_NB * TT * 128; }
+
+// head bits of a thread's items k0 .. k0+cnt-1
+template <int ITEMS, bool SEG>
+__device__ __forceinline__ unsigned row_heads(const SegView &sv, int k0, int cnt) {
+  if (cnt <= 0) return 0u;
+  if (!SEG) return k0 == 0 ? 1u : 0u;
+  const unsigned w = __ldg(sv.bits + (k0 >> 5));
+  unsigned h = (ITEMS == 32) ? w : ((w >> (k0 & 31)) & ((1u << ITEMS) - 1u));
+  if (cnt < ITEMS) h &= (1u << cnt) - 1u;
+  return h;
+}
+// a thread's row: from the TMA tile (128-byte swizzle), or from global memory
+// for the last partial row and past it (identities beyond the vector)
+template <class Op, int ITEMS>
+__device__ __forceinline__ void row_load(typename Op::T (&x)[ITEMS], const unsigned char *buf, int tid, bool in_map,
+                                         const typename Op::T *in, int k0, int cnt) {
+  typedef typename Op::T T;
+  if (in_map) {
+#pragma unroll
+    for (int c = 0; c < 8; c++) {
+      const uint4 u = *(const uint4 *)(buf + swz(tid, c));
+      memcpy(&x[c * (16 / sizeof(T))], &u, 16);
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < ITEMS; i++) x[i] = (i < cnt) ? in[k0 + i] : Op::ident();
+  }
+  if constexpr (std::is_same<Op, CountB>::value) {
+#pragma unroll
+    for (int i = 0; i < ITEMS; i++) x[i] = x[i] != 0;  // pk1_lev counts true flags
+  }
+}
+
+// One thread: the next ticket (-1 once the tiles have run out), and the TMA
+// load of a ticket's tile into its ring slot (a plain arrival for -1).
+__device__ __forceinline__ int ring_ticket(unsigned *counter, int tiles) {
+  const unsigned t = atomicAdd(counter, 1u);
+  return t < (unsigned)tiles ? (int)t : -1;
+}
+__device__ __forceinline__ void ring_arm(int t, unsigned long long *bar, unsigned char *buf, const CUtensorMap *tin,
+                                         unsigned bytes) {
+  if (t >= 0) {
+    mbar_arrive_expect_tx(bar, bytes);
+    tma_load_2d(buf, tin, bar, 0, t * TT);
+  } else {
+    mbar_arrive(bar);
+  }
+}
+// Bound on the waits that make sure a ring slot's load has landed before the
+// slot is armed again or the CTA exits.  They only spin after a load wait
+// already gave up (a timeout is flagged); otherwise the load is long done.
+constexpr int kRingDrain = 1 << 20;
+
+template <class Op, bool SEG>
+__global__ void __launch_bounds__(TB_LB, GCVL_RING_MINB)
+    k_scan_ring(const __grid_constant__ CUtensorMap tin, const __grid_constant__ CUtensorMap tout,
+                TArgs<typename Op::T> a, int tiles) {
+  typedef typename Op::T T;
+  constexpr int ITEMS = row_items<T>(), TILE = TT * ITEMS, NW = TT / 32, NB = RING_NB;
+  constexpr unsigned TILE_BYTES = TILE * sizeof(T);
+  extern __shared__ unsigned char dyn_smem[];
+  unsigned char *ring = (unsigned char *)(((size_t)dyn_smem + 1023) & ~(size_t)1023);
+  __shared__ unsigned long long bar[NB];
+  __shared__ int s_tile[NB];
+  __shared__ int s_wf[NW];
+  __shared__ T s_wv[NW];
+  __shared__ int s_wpf[2][NW];  // per tile (round parity): exclusive prefixes of the warps
+  __shared__ T s_wpv[2][NW];
+  __shared__ int s_af[2];       // per tile: has a segment start, and its aggregate
+  __shared__ T s_av[2];
+  __shared__ T s_P[2];          // carry into the tile being written
+  __shared__ int s_armed[NB];   // per slot: the last round its load was armed for
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+
+  if (tid == TT) {
+#pragma unroll
+    for (int j = 0; j < NB; j++) mbar_init(&bar[j], 1);
+    fence_mbar_init();
+#pragma unroll
+    for (int j = 0; j < NB; j++) {
+      s_tile[j] = ring_ticket(a.lb.counter, tiles);
+      s_armed[j] = j;
+      ring_arm(s_tile[j], &bar[j], ring + j * TILE_BYTES, &tin, TILE_BYTES);
+    }
+  }
+  __syncthreads();
+
+  int lim = a.spin_limit;  // after one timeout the remaining waits give up at once
+  int prev = -1;           // tile folded last round: its outputs are written this round
+  unsigned p_heads = 0;    // this thread's state for it
+  int p_ef = 0;
+  T p_ev = Op::ident();
+  for (int r = 0;; r++) {
+    const int slot = r % NB, pb = r & 1;
+    if (!mbar_wait(&bar[slot], (unsigned)(r / NB) & 1u, lim)) {
+      atomicOr(a.status, DEV_TIMEOUT);
+      lim = 1;
+    }
+    // Written before a CTA barrier that every thread has passed since, so the
+    // round's tile is the same for all threads even when a wait gave up.
+    const int t = s_tile[slot];
+    if (t < 0 && prev < 0) break;
+    const int ps = (r + NB - 1) % NB;  // slot of last round's tile
+
+    unsigned c_heads = 0;
+    int c_ef = 0;
+    T c_ev = Op::ident();
+    if (warp < NW) {
+      // ---------------------------------------------- fold this round's tile
+      if (t >= 0) {
+        const int k0 = t * TILE + tid * ITEMS;
+        const int cnt = max(0, min(ITEMS, a.n - k0));
+        c_heads = row_heads<ITEMS, SEG>(a.sv, k0, cnt);
+        T x[ITEMS];
+        row_load<Op, ITEMS>(x, ring + slot * TILE_BYTES, tid, (long)t * TT + tid < a.rows, a.in, k0, cnt);
+        int tf;
+        T tv;
+        Engine<Op, ITEMS>::agg(x, c_heads, cnt, tf, tv);
+        int f = tf;
+        T v = tv;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+          const int f2 = shfl_up(f, d);
+          const T v2 = shfl_up(v, d);
+          if (lane >= d) { v = f ? v : Op::apply(v2, v); f |= f2; }
+        }
+        c_ef = shfl_up(f, 1);
+        c_ev = shfl_up(v, 1);
+        if (lane == 0) { c_ef = 0; c_ev = Op::ident(); }
+        if (lane == 31) { s_wf[warp] = f; s_wv[warp] = v; }
+      }
+      named_sync(2, TT);
+      if (warp == 0 && t >= 0) {
+        int wf = lane < NW ? s_wf[lane] : 0;
+        T wv = lane < NW ? s_wv[lane] : Op::ident();
+#pragma unroll
+        for (int d = 1; d < NW; d <<= 1) {
+          const int f2 = shfl_up(wf, d);
+          const T v2 = shfl_up(wv, d);
+          if (lane >= d) { wv = wf ? wv : Op::apply(v2, wv); wf |= f2; }
+        }
+        int xf = shfl_up(wf, 1);
+        T xv = shfl_up(wv, 1);
+        if (lane == 0) { xf = 0; xv = Op::ident(); }
+        if (lane < NW) { s_wpf[pb][lane] = xf; s_wpv[pb][lane] = xv; }
+        const int af = shfl_idx(wf, NW - 1);
+        const T av = shfl_idx(wv, NW - 1);
+        if (lane == 0) {
+          lb_publish(a.lb.word + t, (t == 0 || af) ? TS_INC : TS_AGG, to_bits<T>(av));
+          s_af[pb] = af;
+          s_av[pb] = av;
+        }
+      }
+    } else if (prev >= 0) {
+      // ------------------------------- look-back warp: carry into last round's tile
+      const long pbase = (long)prev * TILE;
+      const bool first_head = SEG ? ((__ldg(a.sv.bits + (pbase >> 5)) >> (pbase & 31)) & 1u) != 0 : prev == 0;
+      T P = Op::ident();
+      if (prev > 0 && !first_head) {
+        P = lookback_prefix<Op>(a.lb.word, prev, a.status, a.spin_limit);
+        if (lane == 0 && !s_af[pb ^ 1]) lb_publish(a.lb.word + prev, TS_INC, to_bits<T>(Op::apply(P, s_av[pb ^ 1])));
+      }
+      if (lane == 0) s_P[pb] = P;
+    }
+    // the tile for round r-1+NB: its slot's tile entry was last read at the
+    // start of round r-1, before the previous meeting
+    if (tid == 0 && prev >= 0) s_tile[ps] = ring_ticket(a.lb.counter, tiles);
+    named_sync(1, TB_LB);  // carry of last round's tile ready; this tile's aggregate published
+
+    if (warp < NW) {
+      // ------------------------------------------- outputs of last round's tile
+      if (prev >= 0) {
+        const int k0 = prev * TILE + tid * ITEMS;
+        const int cnt = max(0, min(ITEMS, a.n - k0));
+        const bool in_map = (long)prev * TT + tid < a.rows;
+        int pf = s_wpf[pb ^ 1][warp];
+        T pv = s_wpv[pb ^ 1][warp];
+        pv = p_ef ? p_ev : Op::apply(pv, p_ev);
+        pf |= p_ef;
+        T run = pf ? pv : Op::apply(s_P[pb], pv);
+        T x[ITEMS];
+        unsigned char *buf = ring + ps * TILE_BYTES;
+        row_load<Op, ITEMS>(x, buf, tid, in_map, a.in, k0, cnt);
+#pragma unroll
+        for (int i = 0; i < ITEMS; i++) {
+          if ((p_heads >> i) & 1u) run = Op::init();
+          const T y = run;
+          run = Op::apply(run, x[i]);
+          x[i] = y;
+        }
+        if (in_map) {
+#pragma unroll
+          for (int c = 0; c < 8; c++) {
+            uint4 u;
+            memcpy(&u, &x[c * (16 / sizeof(T))], 16);
+            *(uint4 *)(buf + swz(tid, c)) = u;
+          }
+        } else {
+#pragma unroll
+          for (int i = 0; i < ITEMS; i++)
+            if (i < cnt) a.out[k0 + i] = x[i];
+        }
+        fence_proxy_async_smem();
+        named_sync(2, TT);
+        if (tid == 0) {
+          tma_store_2d(&tout, buf, 0, prev * TT);
+          bulk_commit();
+          bulk_wait_read_all();  // the slot is free once the store has read it
+          if (!mbar_wait(&bar[ps], (unsigned)((r - 1) / NB) & 1u, kRingDrain)) atomicOr(a.status, DEV_TIMEOUT);
+          s_armed[ps] = r - 1 + NB;
+          ring_arm(s_tile[ps], &bar[ps], buf, &tin, TILE_BYTES);
+        }
+      }
+    }
+    prev = t;
+    p_heads = c_heads;
+    p_ef = c_ef;
+    p_ev = c_ev;
+  }
+  // no load may still be landing in the ring when the CTA exits
+  if (tid == 0) {
+#pragma unroll
+    for (int j = 0; j < NB; j++)
+      if (!mbar_wait(&bar[j], (unsigned)(s_armed[j] / NB) & 1u, kRingDrain)) atomicOr(a.status, DEV_TIMEOUT);
+  }
+}
+
 // Second pass of a segmented reduction: the carry into every tile is the
 // segmented exclusive scan of the tile aggregates (status TS_INC marks a
 // tile holding a segment start; its value is the fold from its last start);
@@ -810,6 +1061,28 @@ template <class T> constexpr size_t tma_smem(int wmax) {
   return 1024 + (size_t)TT * row_items<T>() * sizeof(T) + (size_t)(wmax > 0 ? wpad(wmax) + 1 : 0) * 4;
 }
 
+// CTAs of a ring scan: as many as are resident at once (0: it does not fit)
+template <class Op, bool SEG> int ring_grid(int tiles) {
+  static int per_sm = -1;
+  if (per_sm < 0) {
+    int nb = 0;
+    const size_t smem = ring_smem<typename Op::T>();
+    if (smem > 48 * 1024 &&
+        cudaFuncSetAttribute(k_scan_ring<Op, SEG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+            cudaSuccess) {
+      cudaGetLastError();
+      per_sm = 0;
+    } else if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_scan_ring<Op, SEG>, TB_LB, smem) != cudaSuccess) {
+      cudaGetLastError();
+      per_sm = 0;
+    } else {
+      per_sm = nb;
+    }
+  }
+  const long g = (long)per_sm * (st().sm_count > 0 ? st().sm_count : 152);
+  return (int)(g < tiles ? g : tiles);
+}
+
 // Returns false (nothing launched) when the vectors do not suit TMA.
 template <class Op, int MODE, bool SEG>
 bool run_scan_tma(typename Op::T *out, const typename Op::T *in, vec_p sd, int n, int m, vec_p scratch,
@@ -836,6 +1109,14 @@ bool run_scan_tma(typename Op::T *out, const typename Op::T *in, vec_p sd, int n
   GCVL_CK(cudaMemsetAsync(mem, 0, lookback_clear_bytes(tiles), S.stream));
   if (MODE == M_REDUCE) GCVL_CK(cudaMemsetAsync(a.lead, 0xFF, (size_t)tiles * 4, S.stream));
   a.wmax = SEG ? wmax_for<T, MODE>(n, m) : 0;
+  if constexpr (MODE == M_SCAN) {
+    const int grid = ring_grid<Op, SEG>(tiles);
+    if (grid > 0) {
+      k_scan_ring<Op, SEG><<<grid, TB_LB, ring_smem<T>(), S.stream>>>(tin, tout, a, tiles);
+      launch_check(name);
+      return true;
+    }
+  }
   k_scan_tma<Op, MODE, SEG><<<tiles, cta_threads<MODE>(), tma_smem<T>(a.wmax), S.stream>>>(tin, tout, a);
   launch_check(name);
   if (MODE == M_REDUCE) launch_tile_fix<Op>(a.lb.word, a.lead, tiles, out);
