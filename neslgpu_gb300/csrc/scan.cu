@@ -691,15 +691,26 @@ __global__ void __launch_bounds__(cta_threads<MODE>(), MODE == M_REDUCE ? (sizeo
 // ahead in a ring of tile buffers.  Every tile below a ticket already belongs
 // to a running CTA that folds it without waiting on anything but its own
 // load, so the look-back ends however many CTAs are resident.
+//
+// Shape (float64 segmented scan at 2^28): 64-row tiles, two ring slots and
+// 12 CTAs per SM (0.994 ms) over 128-row tiles at 6 per SM (1.020 ms); a
+// third slot (prefetching a round further) costs the CTAs it displaces
+// (1.17-1.23 ms).  The look-back is no longer the limit: skipping it
+// entirely gives 0.999 ms at 128 rows.
 // ============================================================================
 #ifndef GCVL_RING_NB
 #define GCVL_RING_NB 2
 #endif
 #ifndef GCVL_RING_MINB
-#define GCVL_RING_MINB 6
+#define GCVL_RING_MINB 12
+#endif
+#ifndef GCVL_RING_TT
+#define GCVL_RING_TT 64
 #endif
 constexpr int RING_NB = GCVL_RING_NB;
-template <class T> constexpr size_t ring_smem() { return 1024 + (size_t)RING_NB * TT * 128; }
+constexpr int RTT = GCVL_RING_TT;  // rows per tile = compute threads per CTA
+constexpr int RTB = RTT + 32;      // and the look-back warp
+template <class T> constexpr size_t ring_smem() { return 1024 + (size_t)RING_NB * RTT * 128; }
 
 // head bits of a thread's items k0 .. k0+cnt-1
 template <int ITEMS, bool SEG>
@@ -733,6 +744,64 @@ __device__ __forceinline__ void row_load(typename Op::T (&x)[ITEMS], const unsig
   }
 }
 
+// Fold and warp scan of float64 + rows, both in 64-bit fixed point.  A
+// thread's fold from its last segment start is an integer at the scale of
+// its largest exponent (fx_add); the segmented warp scan combines two ranges
+// at the larger of their scales, the other one's integer shifted down to it
+// (truncated), so every prefix is held at the scale of the largest item it
+// contains: its error stays under 32 units of that scale, a few 1e-15 of the
+// sum of magnitudes.  Sixteen 53-bit items take 57 bits and 32 lanes 62, so
+// nothing overflows.  Only the exclusive prefix of each thread and the warp
+// total become doubles, which takes the scan's five FP64 adds per thread off
+// GB300's narrow FP64 pipe.  A warp holding an infinity or NaN scans in FP64.
+template <int ITEMS>
+__device__ __forceinline__ void fold_scan_addd(const double (&x)[ITEMS], unsigned heads, int cnt, int lane, int &f,
+                                               double &v, int &ef, double &ev) {
+  const int from = heads ? 31 - __clz((int)heads) : 0;
+  int emax = 1;
+#pragma unroll
+  for (int i = 0; i < ITEMS; i++)
+    if (i >= from && i < cnt) emax = max(emax, fx_exp((unsigned long long)__double_as_longlong(x[i])));
+  f = heads != 0;
+  if (__any_sync(0xffffffffu, emax == 2047)) {
+    Engine<AddD, ITEMS>::agg(x, heads, cnt, f, v);
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const int f2 = shfl_up(f, d);
+      const double v2 = shfl_up(v, d);
+      if (lane >= d) { v = f ? v : AddD::apply(v2, v); f |= f2; }
+    }
+    ef = shfl_up(f, 1);
+    ev = shfl_up(v, 1);
+    if (lane == 0) { ef = 0; ev = AddD::ident(); }
+    return;
+  }
+  long long acc = 0;
+#pragma unroll
+  for (int i = 0; i < ITEMS; i++)
+    if (i >= from && i < cnt) fx_add(acc, (unsigned long long)__double_as_longlong(x[i]), emax);
+  int e = emax;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const int f2 = shfl_up(f, d), e2 = shfl_up(e, d);
+    const long long a2 = shfl_up(acc, d);
+    if (lane >= d) {
+      if (!f) {
+        const int em = max(e, e2);
+        acc = (acc >> min(em - e, 63)) + (a2 >> min(em - e2, 63));
+        e = em;
+      }
+      f |= f2;
+    }
+  }
+  ef = shfl_up(f, 1);
+  const long long ea = shfl_up(acc, 1);
+  const int ee = shfl_up(e, 1);
+  ev = lane == 0 ? AddD::ident() : fx_to_double_alu(ea, ee);
+  if (lane == 0) ef = 0;
+  v = lane == 31 ? fx_to_double_alu(acc, e) : 0.0;  // the warp total (lane 31 only)
+}
+
 // One thread: the next ticket (-1 once the tiles have run out), and the TMA
 // load of a ticket's tile into its ring slot (a plain arrival for -1).
 __device__ __forceinline__ int ring_ticket(unsigned *counter, int tiles) {
@@ -743,7 +812,7 @@ __device__ __forceinline__ void ring_arm(int t, unsigned long long *bar, unsigne
                                          unsigned bytes) {
   if (t >= 0) {
     mbar_arrive_expect_tx(bar, bytes);
-    tma_load_2d(buf, tin, bar, 0, t * TT);
+    tma_load_2d(buf, tin, bar, 0, t * RTT);
   } else {
     mbar_arrive(bar);
   }
@@ -754,11 +823,11 @@ __device__ __forceinline__ void ring_arm(int t, unsigned long long *bar, unsigne
 constexpr int kRingDrain = 1 << 20;
 
 template <class Op, bool SEG>
-__global__ void __launch_bounds__(TB_LB, GCVL_RING_MINB)
+__global__ void __launch_bounds__(RTB, GCVL_RING_MINB)
     k_scan_ring(const __grid_constant__ CUtensorMap tin, const __grid_constant__ CUtensorMap tout,
                 TArgs<typename Op::T> a, int tiles) {
   typedef typename Op::T T;
-  constexpr int ITEMS = row_items<T>(), TILE = TT * ITEMS, NW = TT / 32, NB = RING_NB;
+  constexpr int ITEMS = row_items<T>(), TILE = RTT * ITEMS, NW = RTT / 32, NB = RING_NB;
   constexpr unsigned TILE_BYTES = TILE * sizeof(T);
   extern __shared__ unsigned char dyn_smem[];
   unsigned char *ring = (unsigned char *)(((size_t)dyn_smem + 1023) & ~(size_t)1023);
@@ -774,7 +843,7 @@ __global__ void __launch_bounds__(TB_LB, GCVL_RING_MINB)
   __shared__ int s_armed[NB];   // per slot: the last round its load was armed for
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
-  if (tid == TT) {
+  if (tid == RTT) {
 #pragma unroll
     for (int j = 0; j < NB; j++) mbar_init(&bar[j], 1);
     fence_mbar_init();
@@ -814,24 +883,26 @@ __global__ void __launch_bounds__(TB_LB, GCVL_RING_MINB)
         const int cnt = max(0, min(ITEMS, a.n - k0));
         c_heads = row_heads<ITEMS, SEG>(a.sv, k0, cnt);
         T x[ITEMS];
-        row_load<Op, ITEMS>(x, ring + slot * TILE_BYTES, tid, (long)t * TT + tid < a.rows, a.in, k0, cnt);
-        int tf;
-        T tv;
-        Engine<Op, ITEMS>::agg(x, c_heads, cnt, tf, tv);
-        int f = tf;
-        T v = tv;
+        row_load<Op, ITEMS>(x, ring + slot * TILE_BYTES, tid, (long)t * RTT + tid < a.rows, a.in, k0, cnt);
+        int f;
+        T v;
+        if constexpr (std::is_same<Op, AddD>::value) {
+          fold_scan_addd<ITEMS>(x, c_heads, cnt, lane, f, v, c_ef, c_ev);
+        } else {
+          Engine<Op, ITEMS>::agg(x, c_heads, cnt, f, v);
 #pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-          const int f2 = shfl_up(f, d);
-          const T v2 = shfl_up(v, d);
-          if (lane >= d) { v = f ? v : Op::apply(v2, v); f |= f2; }
+          for (int d = 1; d < 32; d <<= 1) {
+            const int f2 = shfl_up(f, d);
+            const T v2 = shfl_up(v, d);
+            if (lane >= d) { v = f ? v : Op::apply(v2, v); f |= f2; }
+          }
+          c_ef = shfl_up(f, 1);
+          c_ev = shfl_up(v, 1);
+          if (lane == 0) { c_ef = 0; c_ev = Op::ident(); }
         }
-        c_ef = shfl_up(f, 1);
-        c_ev = shfl_up(v, 1);
-        if (lane == 0) { c_ef = 0; c_ev = Op::ident(); }
         if (lane == 31) { s_wf[warp] = f; s_wv[warp] = v; }
       }
-      named_sync(2, TT);
+      named_sync(2, RTT);
       if (warp == 0 && t >= 0) {
         int wf = lane < NW ? s_wf[lane] : 0;
         T wv = lane < NW ? s_wv[lane] : Op::ident();
@@ -867,14 +938,14 @@ __global__ void __launch_bounds__(TB_LB, GCVL_RING_MINB)
     // the tile for round r-1+NB: its slot's tile entry was last read at the
     // start of round r-1, before the previous meeting
     if (tid == 0 && prev >= 0) s_tile[ps] = ring_ticket(a.lb.counter, tiles);
-    named_sync(1, TB_LB);  // carry of last round's tile ready; this tile's aggregate published
+    named_sync(1, RTB);  // carry of last round's tile ready; this tile's aggregate published
 
     if (warp < NW) {
       // ------------------------------------------- outputs of last round's tile
       if (prev >= 0) {
         const int k0 = prev * TILE + tid * ITEMS;
         const int cnt = max(0, min(ITEMS, a.n - k0));
-        const bool in_map = (long)prev * TT + tid < a.rows;
+        const bool in_map = (long)prev * RTT + tid < a.rows;
         int pf = s_wpf[pb ^ 1][warp];
         T pv = s_wpv[pb ^ 1][warp];
         pv = p_ef ? p_ev : Op::apply(pv, p_ev);
@@ -903,9 +974,9 @@ __global__ void __launch_bounds__(TB_LB, GCVL_RING_MINB)
             if (i < cnt) a.out[k0 + i] = x[i];
         }
         fence_proxy_async_smem();
-        named_sync(2, TT);
+        named_sync(2, RTT);
         if (tid == 0) {
-          tma_store_2d(&tout, buf, 0, prev * TT);
+          tma_store_2d(&tout, buf, 0, prev * RTT);
           bulk_commit();
           bulk_wait_read_all();  // the slot is free once the store has read it
           if (!mbar_wait(&bar[ps], (unsigned)((r - 1) / NB) & 1u, kRingDrain)) atomicOr(a.status, DEV_TIMEOUT);
@@ -1025,12 +1096,12 @@ static EncodeTiledFn encode_tiled() {
   return fn;
 }
 
-template <class T> bool tma_map(CUtensorMap *map, const void *ptr, long rows) {
+template <class T> bool tma_map(CUtensorMap *map, const void *ptr, long rows, int box_rows = TT) {
   EncodeTiledFn enc = encode_tiled();
   if (!enc) return false;
   cuuint64_t dims[2] = {(cuuint64_t)row_items<T>(), (cuuint64_t)rows};
   cuuint64_t strides[1] = {128};
-  cuuint32_t box[2] = {(cuuint32_t)row_items<T>(), (cuuint32_t)TT};
+  cuuint32_t box[2] = {(cuuint32_t)row_items<T>(), (cuuint32_t)box_rows};
   cuuint32_t es[2] = {1, 1};
   CUresult r = enc(
       map, sizeof(T) == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_INT32, 2, (void *)ptr,
@@ -1072,7 +1143,7 @@ template <class Op, bool SEG> int ring_grid(int tiles) {
             cudaSuccess) {
       cudaGetLastError();
       per_sm = 0;
-    } else if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_scan_ring<Op, SEG>, TB_LB, smem) != cudaSuccess) {
+    } else if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_scan_ring<Op, SEG>, RTB, smem) != cudaSuccess) {
       cudaGetLastError();
       per_sm = 0;
     } else {
@@ -1092,10 +1163,29 @@ bool run_scan_tma(typename Op::T *out, const typename Op::T *in, vec_p sd, int n
   const long rows = (long)n / row_items<T>();
   if (rows < 1 || ((size_t)in & 15) || (MODE == M_SCAN && ((size_t)out & 15))) return false;
   CUtensorMap tin, tout;
+  State &S = st();
+  if constexpr (MODE == M_SCAN) {
+    const int tiles = ceil_div(n, (long)RTT * row_items<T>());
+    const int grid = ring_grid<Op, SEG>(tiles);
+    if (grid > 0) {
+      if (!tma_map<T>(&tin, in, rows, RTT) || !tma_map<T>(&tout, out, rows, RTT)) return false;
+      void *mem = scratch_or_work(scratch, lookback_bytes(tiles));
+      if (!mem) return true;
+      TArgs<T> a{};
+      a.out = out; a.in = in; a.n = n; a.rows = rows;
+      a.sv = SEG ? seg_view(sd, n, m) : SegView{nullptr, nullptr, nullptr, nullptr, n, 1};
+      a.lb = lookback_carve(mem, tiles);
+      a.status = S.d_status;
+      a.spin_limit = S.spin_limit;
+      GCVL_CK(cudaMemsetAsync(mem, 0, lookback_clear_bytes(tiles), S.stream));
+      k_scan_ring<Op, SEG><<<grid, RTB, ring_smem<T>(), S.stream>>>(tin, tout, a, tiles);
+      launch_check(name);
+      return true;
+    }
+  }
   if (!tma_map<T>(&tin, in, rows)) return false;
   if (MODE == M_SCAN) { if (!tma_map<T>(&tout, out, rows)) return false; }
   else tout = tin;
-  State &S = st();
   const int tiles = ceil_div(n, (long)TT * row_items<T>());
   void *mem = scratch_or_work(scratch, reduce_pass_bytes(tiles));
   if (!mem) return true;
@@ -1109,14 +1199,6 @@ bool run_scan_tma(typename Op::T *out, const typename Op::T *in, vec_p sd, int n
   GCVL_CK(cudaMemsetAsync(mem, 0, lookback_clear_bytes(tiles), S.stream));
   if (MODE == M_REDUCE) GCVL_CK(cudaMemsetAsync(a.lead, 0xFF, (size_t)tiles * 4, S.stream));
   a.wmax = SEG ? wmax_for<T, MODE>(n, m) : 0;
-  if constexpr (MODE == M_SCAN) {
-    const int grid = ring_grid<Op, SEG>(tiles);
-    if (grid > 0) {
-      k_scan_ring<Op, SEG><<<grid, TB_LB, ring_smem<T>(), S.stream>>>(tin, tout, a, tiles);
-      launch_check(name);
-      return true;
-    }
-  }
   k_scan_tma<Op, MODE, SEG><<<tiles, cta_threads<MODE>(), tma_smem<T>(a.wmax), S.stream>>>(tin, tout, a);
   launch_check(name);
   if (MODE == M_REDUCE) launch_tile_fix<Op>(a.lb.word, a.lead, tiles, out);
@@ -1133,7 +1215,8 @@ template <class T> constexpr int tile_elems() { return Tiling<T>::BLOCK * Tiling
 
 template <class T> int scan_units(int n) {
   if (n <= 0) return 0;
-  return lookback_units(ceil_div(n, tile_elems<T>()));
+  const int a = ceil_div(n, tile_elems<T>()), b = ceil_div(n, RTT * row_items<T>());
+  return lookback_units(a > b ? a : b);
 }
 
 // Shared launcher.  `sd` may be null for unsegmented modes.
