@@ -175,7 +175,7 @@ class Gpu:
         return self.c.gcvl_event_elapsed_ms(a, b)
 
 
-def timed(g, fn, reps=5):
+def timed(g, fn, reps=10):
     """Median CUDA-event time (ms) of fn() after one warm-up call."""
     fn()
     e = g.events(2)

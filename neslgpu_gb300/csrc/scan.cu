@@ -356,6 +356,15 @@ __device__ __forceinline__ void agg_add_split(const double (&x)[ITEMS], unsigned
   constexpr int H = GCVL_RED_FX_ITEMS < ITEMS ? GCVL_RED_FX_ITEMS : ITEMS;  // items in fixed point
   tf = heads != 0;
   tv = AddD::ident();
+  if (__all_sync(0xffffffffu, heads == 0 && cnt == ITEMS)) {
+    // the whole warp folds full rows without segment starts: no per-item tests
+    const double lo = fx_range_part<ITEMS, 0, H>(x, 0, ITEMS);
+    double hi = -0.0;
+#pragma unroll
+    for (int i = H; i < ITEMS; i++) hi = __dadd_rn(hi, x[i]);
+    tv = __dadd_rn(lo, hi);
+    return;
+  }
   if (cnt <= 0) return;
   const int from = heads ? 31 - __clz((int)heads) : 0;
   const double lo = fx_range_part<ITEMS, 0, H>(x, from, cnt);
@@ -712,16 +721,6 @@ constexpr int RTT = GCVL_RING_TT;  // rows per tile = compute threads per CTA
 constexpr int RTB = RTT + 32;      // and the look-back warp
 template <class T> constexpr size_t ring_smem() { return 1024 + (size_t)RING_NB * RTT * 128; }
 
-// head bits of a thread's items k0 .. k0+cnt-1
-template <int ITEMS, bool SEG>
-__device__ __forceinline__ unsigned row_heads(const SegView &sv, int k0, int cnt) {
-  if (cnt <= 0) return 0u;
-  if (!SEG) return k0 == 0 ? 1u : 0u;
-  const unsigned w = __ldg(sv.bits + (k0 >> 5));
-  unsigned h = (ITEMS == 32) ? w : ((w >> (k0 & 31)) & ((1u << ITEMS) - 1u));
-  if (cnt < ITEMS) h &= (1u << cnt) - 1u;
-  return h;
-}
 // a thread's row: from the TMA tile (128-byte swizzle), or from global memory
 // for the last partial row and past it (identities beyond the vector)
 template <class Op, int ITEMS>
@@ -757,11 +756,17 @@ __device__ __forceinline__ void row_load(typename Op::T (&x)[ITEMS], const unsig
 template <int ITEMS>
 __device__ __forceinline__ void fold_scan_addd(const double (&x)[ITEMS], unsigned heads, int cnt, int lane, int &f,
                                                double &v, int &ef, double &ev) {
+  const bool plain = __all_sync(0xffffffffu, heads == 0 && cnt == ITEMS);  // no per-item tests
   const int from = heads ? 31 - __clz((int)heads) : 0;
   int emax = 1;
+  if (plain) {
 #pragma unroll
-  for (int i = 0; i < ITEMS; i++)
-    if (i >= from && i < cnt) emax = max(emax, fx_exp((unsigned long long)__double_as_longlong(x[i])));
+    for (int i = 0; i < ITEMS; i++) emax = max(emax, fx_exp((unsigned long long)__double_as_longlong(x[i])));
+  } else {
+#pragma unroll
+    for (int i = 0; i < ITEMS; i++)
+      if (i >= from && i < cnt) emax = max(emax, fx_exp((unsigned long long)__double_as_longlong(x[i])));
+  }
   f = heads != 0;
   if (__any_sync(0xffffffffu, emax == 2047)) {
     Engine<AddD, ITEMS>::agg(x, heads, cnt, f, v);
@@ -777,9 +782,14 @@ __device__ __forceinline__ void fold_scan_addd(const double (&x)[ITEMS], unsigne
     return;
   }
   long long acc = 0;
+  if (plain) {
 #pragma unroll
-  for (int i = 0; i < ITEMS; i++)
-    if (i >= from && i < cnt) fx_add(acc, (unsigned long long)__double_as_longlong(x[i]), emax);
+    for (int i = 0; i < ITEMS; i++) fx_add(acc, (unsigned long long)__double_as_longlong(x[i]), emax);
+  } else {
+#pragma unroll
+    for (int i = 0; i < ITEMS; i++)
+      if (i >= from && i < cnt) fx_add(acc, (unsigned long long)__double_as_longlong(x[i]), emax);
+  }
   int e = emax;
 #pragma unroll
   for (int d = 1; d < 32; d <<= 1) {
@@ -857,6 +867,10 @@ __global__ void __launch_bounds__(RTB, GCVL_RING_MINB)
   __syncthreads();
 
   int lim = a.spin_limit;  // after one timeout the remaining waits give up at once
+  // head-bit word of this thread's row in the coming round's tile, read a
+  // round ahead (the bitmap is too large to stay in L2)
+  unsigned nx_word = 0;
+  if (SEG && warp < NW && s_tile[0] >= 0) nx_word = __ldg(a.sv.bits + ((s_tile[0] * TILE + tid * ITEMS) >> 5));
   int prev = -1;           // tile folded last round: its outputs are written this round
   unsigned p_heads = 0;    // this thread's state for it
   int p_ef = 0;
@@ -881,7 +895,14 @@ __global__ void __launch_bounds__(RTB, GCVL_RING_MINB)
       if (t >= 0) {
         const int k0 = t * TILE + tid * ITEMS;
         const int cnt = max(0, min(ITEMS, a.n - k0));
-        c_heads = row_heads<ITEMS, SEG>(a.sv, k0, cnt);
+        if (cnt > 0) {
+          if (SEG) {
+            c_heads = (ITEMS == 32) ? nx_word : ((nx_word >> (k0 & 31)) & ((1u << ITEMS) - 1u));
+            if (cnt < ITEMS) c_heads &= (1u << cnt) - 1u;
+          } else {
+            c_heads = k0 == 0 ? 1u : 0u;
+          }
+        }
         T x[ITEMS];
         row_load<Op, ITEMS>(x, ring + slot * TILE_BYTES, tid, (long)t * RTT + tid < a.rows, a.in, k0, cnt);
         int f;
@@ -941,6 +962,12 @@ __global__ void __launch_bounds__(RTB, GCVL_RING_MINB)
     named_sync(1, RTB);  // carry of last round's tile ready; this tile's aggregate published
 
     if (warp < NW) {
+      // the next round's tile (its ticket was taken before an earlier meeting)
+      if (SEG) {
+        const int tn = s_tile[(r + 1) % NB];
+        const int kn = tn * TILE + tid * ITEMS;
+        if (tn >= 0 && kn < a.n) nx_word = __ldg(a.sv.bits + (kn >> 5));
+      }
       // ------------------------------------------- outputs of last round's tile
       if (prev >= 0) {
         const int k0 = prev * TILE + tid * ITEMS;
