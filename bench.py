@@ -53,7 +53,7 @@ sys.path.insert(0, str(ROOT))
 LOG2N = 28
 SEED = 0x5EED + 1
 METRIC = "CVL primitive Gelem/s (segmented +_scan and +_reduce, float64)"
-NCU_SCAN_DRAM_BYTES_PER_ELEM = 503.19e6 / (1 << 25)  # add_sed's DRAM traffic per element, ncu at 2^25
+NCU_SCAN_DRAM_BYTES_PER_ELEM = 488.69e6 / (1 << 25)  # add_sed's DRAM traffic per element, ncu at 2^25
 UNIT = "Gelem/s"
 
 
@@ -640,10 +640,10 @@ def gpu_arm(a):
     alg_bytes = 16.0 * n + 4.0 * m
     achieved = alg_bytes / (t_sed * 1e-3) / 1e9
     # DRAM bytes per launch: dram__bytes_read.sum + dram__bytes_write.sum of
-    # one ncu capture of this kernel at 2^25 elements (503 MB), scaled by the
-    # elements to this launch (profiles/k_scan_tma_add_sed_add_red_2e25.md)
+    # one ncu capture of this kernel at 2^25 elements (489 MB), scaled by the
+    # elements to this launch (profiles/k_scan_ring_add_sed_k_scan_tma_add_red_2e25.md)
     traffic = round(NCU_SCAN_DRAM_BYTES_PER_ELEM * n)
-    roofline = {"bound": "hbm", "kernel": "k_scan_tma<AddD,scan,segmented> (add_sed)",
+    roofline = {"bound": "hbm", "kernel": "k_scan_ring<AddD,segmented> (add_sed)",
                 "achieved": round(achieved, 1), "peak": hbm, "peak_kind": peak_kind, "unit": "GB/s",
                 "frac": round(achieved / hbm, 4), "traffic": traffic,
                 "traffic_source": "ncu capture at 2^25 elements, scaled by the elements",
