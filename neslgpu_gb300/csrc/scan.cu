@@ -1392,8 +1392,8 @@ void run_reduce(const typename Op::T *in, int n, typename Op::T *result_dev, vec
 // fix-up list, or the generic kernel's look-back area
 template <class T> int seg_reduce_units(int n) {
   if (n <= 0) return 0;
-  const int tiles = ceil_div(n, tile_elems<T>());
-  return (int)((reduce_pass_bytes(tiles) + 7) / 8);
+  const int a = ceil_div(n, tile_elems<T>()), b = ceil_div(n, TT * row_items<T>());
+  return (int)((reduce_pass_bytes(a > b ? a : b) + 7) / 8);
 }
 template <class T> int reduce_units(int n) {
   (void)n;
