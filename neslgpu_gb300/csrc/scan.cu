@@ -342,6 +342,14 @@ template <int ITEMS> struct Engine<AddD, ITEMS> {
   }
 };
 
+// Float64 + reductions of short segments (the CHAIN form of the kernel,
+// chosen when segments average under RED_CHAIN_MEAN elements): a warp in
+// which some thread ends at least two segments sums its pieces with one FP64
+// add per item instead of a fixed-point pass per segment end.  At 2^28,
+// geometric(4) segments 2.98 -> 1.14 ms, geometric(64) 1.12 -> 1.01 ms; the
+// log-normal(5,2) bench segments (about 1100 elements on average) keep the
+// plain form, which the chain's code alone slows by 2-4 %.
+constexpr long RED_CHAIN_MEAN = 256;
 // Reductions: a thread's float64 + fold split between the integer pipes
 // (the first GCVL_RED_FX_ITEMS items, fixed point) and the FP64 pipe (the
 // rest, an add chain), so that neither carries the whole fold; 14 of 16
@@ -400,7 +408,7 @@ template <int MODE> constexpr int cta_threads() { return MODE == M_REDUCE ? TT :
 #ifndef GCVL_RED_MINB_Z
 #define GCVL_RED_MINB_Z 8
 #endif
-template <class Op, int MODE, bool SEG>
+template <class Op, int MODE, bool SEG, bool CHAIN = false>
 __global__ void __launch_bounds__(cta_threads<MODE>(), MODE == M_REDUCE ? (sizeof(typename Op::T) == 8 ? GCVL_RED_MINB_D : GCVL_RED_MINB_Z) : GCVL_SCAN_MINB) k_scan_tma(const __grid_constant__ CUtensorMap tin,
                                                      const __grid_constant__ CUtensorMap tout,
                                                      TArgs<typename Op::T> a) {
@@ -649,6 +657,27 @@ __global__ void __launch_bounds__(cta_threads<MODE>(), MODE == M_REDUCE ? (sizeo
         const int kn = k0 + cnt;
         const unsigned nh = kn >= a.n ? 1u : (__ldg(a.sv.bits + (kn >> 5)) >> (kn & 31)) & 1u;
         unsigned ends = ((heads >> 1) | (nh << (cnt - 1))) & (cnt >= 32 ? ~0u : ((1u << cnt) - 1u));
+        if (CHAIN && __any_sync(0xffffffffu, __popc(ends) >= 2)) {
+          // short segments: one FP64 add per item beats a fixed-point pass
+          // per segment end (each a separate sum of up to 16 items)
+          double r = run;
+#pragma unroll
+          for (int i = 0; i < ITEMS; i++) {
+            if (i < cnt) {
+              if ((heads >> i) & 1u) r = 0.0;
+              r = __dadd_rn(r, x[i]);
+              if ((ends >> i) & 1u) {
+                a.out[s] = r;
+                if (!pf && !(heads & ((2u << i) - 1u))) a.lead[tile] = s;  // began in an earlier tile
+                int s2 = s + 1;
+                while (s2 < m && off(s2 + 1) == end) { a.out[s2] = 0.0; ++s2; }
+                s = s2;
+                if (s < m) end = off(s + 1);
+              }
+            }
+          }
+          ends = 0;
+        }
         int ps = 0;
         while (ends) {
           const int i = __ffs(ends) - 1;
@@ -1226,7 +1255,13 @@ bool run_scan_tma(typename Op::T *out, const typename Op::T *in, vec_p sd, int n
   GCVL_CK(cudaMemsetAsync(mem, 0, lookback_clear_bytes(tiles), S.stream));
   if (MODE == M_REDUCE) GCVL_CK(cudaMemsetAsync(a.lead, 0xFF, (size_t)tiles * 4, S.stream));
   a.wmax = SEG ? wmax_for<T, MODE>(n, m) : 0;
-  k_scan_tma<Op, MODE, SEG><<<tiles, cta_threads<MODE>(), tma_smem<T>(a.wmax), S.stream>>>(tin, tout, a);
+  bool chain = false;
+  if constexpr (MODE == M_REDUCE && SEG && std::is_same<Op, AddD>::value) {
+    chain = (long)n < RED_CHAIN_MEAN * m;
+    if (chain)
+      k_scan_tma<Op, MODE, SEG, true><<<tiles, cta_threads<MODE>(), tma_smem<T>(a.wmax), S.stream>>>(tin, tout, a);
+  }
+  if (!chain) k_scan_tma<Op, MODE, SEG><<<tiles, cta_threads<MODE>(), tma_smem<T>(a.wmax), S.stream>>>(tin, tout, a);
   launch_check(name);
   if (MODE == M_REDUCE) launch_tile_fix<Op>(a.lb.word, a.lead, tiles, out);
   return true;
