@@ -1030,15 +1030,21 @@ __global__ void __launch_bounds__(RTB, GCVL_RING_MINB)
             if (i < cnt) a.out[k0 + i] = x[i];
         }
         fence_proxy_async_smem();
-        named_sync(2, RTT);
-        if (tid == 0) {
-          tma_store_2d(&tout, buf, 0, prev * RTT);
-          bulk_commit();
-          bulk_wait_read_all();  // the slot is free once the store has read it
-          if (!mbar_wait(&bar[ps], (unsigned)((r - 1) / NB) & 1u, kRingDrain)) atomicOr(a.status, DEV_TIMEOUT);
-          s_armed[ps] = r - 1 + NB;
-          ring_arm(s_tile[ps], &bar[ps], buf, &tin, TILE_BYTES);
-        }
+        named_arrive(3, RTB);  // outputs in the slot; the look-back warp stores them
+      }
+    } else if (prev >= 0) {
+      // ------------------------------- look-back warp: store last round's tile
+      // and load the tile for round r-1+NB into its slot, off the compute
+      // warps' path
+      named_sync(3, RTB);
+      if (lane == 0) {
+        unsigned char *buf = ring + ps * TILE_BYTES;
+        tma_store_2d(&tout, buf, 0, prev * RTT);
+        bulk_commit();
+        bulk_wait_read_all();  // the slot is free once the store has read it
+        if (!mbar_wait(&bar[ps], (unsigned)((r - 1) / NB) & 1u, kRingDrain)) atomicOr(a.status, DEV_TIMEOUT);
+        s_armed[ps] = r - 1 + NB;
+        ring_arm(s_tile[ps], &bar[ps], buf, &tin, TILE_BYTES);
       }
     }
     prev = t;
@@ -1047,7 +1053,7 @@ __global__ void __launch_bounds__(RTB, GCVL_RING_MINB)
     p_ev = c_ev;
   }
   // no load may still be landing in the ring when the CTA exits
-  if (tid == 0) {
+  if (tid == RTT) {
 #pragma unroll
     for (int j = 0; j < NB; j++)
       if (!mbar_wait(&bar[j], (unsigned)(s_armed[j] / NB) & 1u, kRingDrain)) atomicOr(a.status, DEV_TIMEOUT);
