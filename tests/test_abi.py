@@ -52,3 +52,28 @@ def test_host_side_functions_without_gpu():
     assert c.add_sez_inplace() == 1
     assert c.rku_luz_scratch(1 << 20) > 0 and c.rku_lez_scratch(1 << 20, 5) > c.rku_luz_scratch(1 << 20)
     assert c.mke_fov_inplace() == 0
+
+
+def _lookback_bytes(tiles):
+    # the look-back area a scan kernel carves from its scratch: 512 bytes of
+    # counter and alignment slack, then 16 bytes per tile rounded to 256
+    return 512 + -(-tiles * 16 // 256) * 256
+
+
+def test_scratch_covers_the_kernels_tiles():
+    """Every scan's scratch holds the look-back area of the persistent ring
+    (tiles of 64 rows of 128 bytes: 1024 doubles or 2048 ints), and every
+    segmented float64 +-reduction's holds the TMA kernel's area, its per-tile
+    list of results to complete and the second pass's look-back (tiles of
+    128 rows); the fused SpMV's the same for its 2048-element tiles."""
+    from neslgpu_gb300.cvl import load
+    c = load()
+    for n in (1, 1000, 1 << 16, (1 << 20) + 7, 1 << 28):
+        for m in (1, max(1, n // 64)):
+            assert 8 * c.add_sed_scratch(n, m) >= _lookback_bytes(-(-n // 1024)), (n, m)
+            assert 8 * c.add_sez_scratch(n, m) >= _lookback_bytes(-(-n // 2048)), (n, m)
+            assert 8 * c.add_sud_scratch(n) >= _lookback_bytes(-(-n // 1024)), n
+            t = -(-n // 2048)
+            red = _lookback_bytes(t) + -(-t * 4 // 256) * 256 + _lookback_bytes(-(-t // 1024))
+            assert 8 * c.add_red_scratch(n, m) >= red, (n, m)
+            assert 8 * c.gcvl_spmv_csr_scratch(n, m) >= red, (n, m)
