@@ -4,13 +4,21 @@
 // scans that restart from the operator's initial value at every segment,
 // reductions that yield the initial value for an empty segment.
 //
-// Design: one single-pass kernel per (operator, mode).  A CTA takes the next
-// tile ticket, stages its tile through shared memory with coalesced loads,
-// folds (head, value) pairs per thread, scans them across the CTA with warp
-// shuffles, and gets the carry from earlier tiles by decoupled look-back.
-// A tile that holds a segment head publishes its inclusive value at once, so
-// with short segments no CTA ever waits; long segments wait on a chain that
-// the warp-wide look-back walks 32 tiles at a time.  Every wait is bounded.
+// Design: tiles of 128-byte rows, one row per thread; a thread folds its
+// (head, value) pairs, warp shuffles scan them across the CTA, and the carry
+// from earlier tiles comes from a decoupled look-back over 16-byte status
+// words (a tile that holds a segment head publishes its inclusive value at
+// once; the warp-wide look-back walks 32 tiles per round trip).  Kernels:
+//  * k_scan_ring -- scans of 16-byte aligned vectors: persistent CTAs take
+//    tiles from a ticket counter, move them by TMA through a two-slot ring,
+//    and write each tile's outputs one round after its fold, so the carry
+//    it needs is ready;
+//  * k_scan_tma -- reductions of 16-byte aligned vectors, one TMA tile per
+//    CTA, results at segment ends and no look-back wait: k_tile_fix
+//    completes the results that span tiles (and the no-alloc scan);
+//  * k_scan -- everything else (vectors off a 16-byte boundary, the offsets
+//    scan of mke_fov), staged with coalesced loads.
+// Every wait is bounded.
 #include "gcvl.cuh"
 #include "tma.cuh"
 
@@ -246,17 +254,18 @@ k_scan(ScanArgs<typename Op::T> a) {
 }
 
 // ============================================================================
-// TMA-staged single-pass kernel (the fast path for 16-byte aligned vectors).
+// TMA-staged tile kernel: the reductions of 16-byte aligned vectors (and the
+// no-alloc entry point's scan).
 //
-// A tile is 256 rows of 128 bytes (32 ints or 16 doubles per row), one row
-// per thread.  One elected thread moves the whole tile with a 2-D TMA tensor
-// copy (128-byte swizzle, so each thread reads its row from shared memory
-// without bank conflicts) and writes scan results back the same way.
-// Segment heads come from a window of the segment offsets that the CTA
-// loads once into shared memory.  Float64 + folds run in 128-bit integer
-// fixed point and float64 min/max compare integer keys, which keeps the
-// GB300's narrow FP64 pipe free for the one add per element that an
-// exclusive scan output needs.
+// A tile is TT rows of 128 bytes (32 ints or 16 doubles per row), one row per
+// thread.  One elected thread moves the whole tile with a 2-D TMA tensor copy
+// (128-byte swizzle, so each thread reads its row from shared memory without
+// bank conflicts) and, for a scan, writes the results back the same way.
+// Segment heads come from the head bitmap; a reduction's segment numbers from
+// a window of the segment offsets that the CTA loads into shared memory.
+// Float64 + folds run in 64-bit integer fixed point and float64 min/max
+// compare integer keys, which keeps GB300's narrow FP64 pipe for the adds
+// that need it.
 // ============================================================================
 #ifndef GCVL_TT
 #define GCVL_TT 128
