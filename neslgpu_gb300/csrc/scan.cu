@@ -906,7 +906,9 @@ __global__ void __launch_bounds__(RTB, GCVL_RING_MINB)
 
   int lim = a.spin_limit;  // after one timeout the remaining waits give up at once
   // head-bit word of this thread's row in the coming round's tile, read a
-  // round ahead (the bitmap is too large to stay in L2)
+  // round ahead (the bitmap is too large to stay in L2).  Rows past the
+  // vector's end in its last tile still read inside the bitmap: it is padded
+  // to 8192-element multiples (segdes_nbits_words), tiles divide that.
   unsigned nx_word = 0;
   if (SEG && warp < NW && s_tile[0] >= 0) nx_word = __ldg(a.sv.bits + ((s_tile[0] * TILE + tid * ITEMS) >> 5));
   int prev = -1;           // tile folded last round: its outputs are written this round
