@@ -777,18 +777,22 @@ int gcvl_pipeline_percall(int is_double, vec_p x, const int *seg_lens_host, cons
                           vec_p sd2, vec_p work, unsigned seed);
 /* Segmented exclusive +-scan of float64 (add_sed) that allocates nothing.
  * No counterpart in the reference.  For callers that may not allocate device
- * memory -- code running during CUDA graph capture, embedders whose device
- * memory all belongs to their own pool, runtimes that forbid allocation
- * after start-up.  Same arguments and results as add_sed minus the scratch
- * vector: the look-back scratch is a fixed array inside the library, sized
- * for n <= gcvl_add_sed_noalloc_max_n() (2^28 elements, about 2.6 MB, held
- * on every GPU that loads the library until exit).  Larger n is rejected
- * with GCVL error 5 (range) and nothing runs.  The first call on a device
- * looks up the array's device address there, so make it before any stream
- * capture.  The library's first-use set-up is not run; the call uses the
- * library stream if that exists, else the legacy default stream.  Calls
- * share the array: calls that overlap on the GPU race.  Returns 0 or a
- * GCVL error code. */
+ * memory: embedders whose device memory all belongs to their own pool, and
+ * runtimes that forbid allocation after start-up (an allocation can
+ * synchronise the device or fail when the caller cannot handle it).  Same
+ * arguments and results as add_sed minus the scratch vector: the look-back
+ * scratch is a fixed array inside the library, sized for
+ * n <= gcvl_add_sed_noalloc_max_n() (2^28 elements; 2,097,664 bytes = 2.0 MiB,
+ * held on every GPU that loads the library until exit).  Larger n is
+ * rejected with GCVL error 5 (range) and nothing runs.  The first call on a
+ * device looks up the array's device address there (kept until exit, so no
+ * call may follow a cudaDeviceReset); make that first call before any
+ * stream capture.  The library's first-use set-up is not run; the call uses
+ * the library stream if that exists, else the legacy default stream.  Calls
+ * share the array: calls that overlap on the GPU race.  Returns 0, or a GCVL
+ * error code when the call could not be issued; a bounded device wait that
+ * gave up is reported by the next gcvl_sync (error 3), as for every other
+ * call. */
 int gcvl_add_sed_noalloc(vec_p d, vec_p s, vec_p sd, int n, int m);
 long gcvl_add_sed_noalloc_max_n(void);
 /* Kernel variants of the segmented scans, reductions and ranks (no

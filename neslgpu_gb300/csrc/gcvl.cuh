@@ -52,6 +52,10 @@ inline cudaStream_t stream() { return st().stream; }
 // library workspace (grown on demand, kept for later calls).
 void *scratch_or_work(vec_p scratch, size_t bytes);
 void launch_check(const char *what);
+// Status word of the no-allocation entry point (scan.cu): whether it has run
+// on the current device, and folding its bits into the error state.
+bool noalloc_used();
+void noalloc_fold_status();
 
 enum ErrorCode {
   GCVL_OK = 0,

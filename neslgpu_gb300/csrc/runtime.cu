@@ -95,11 +95,18 @@ GCVL_EXPORT int gcvl_last_error(void) { return st().err; }
 GCVL_EXPORT const char *gcvl_error_string(void) { return st().msg; }
 GCVL_EXPORT void gcvl_clear_error(void) { st().err = 0; st().msg[0] = 0; }
 
-// Synchronise the library stream, fold the device status word into the
+// Synchronise the library stream, fold the device status words into the
 // error state and return the error code (0 when all is well).
 GCVL_EXPORT int gcvl_sync(void) {
-  ensure_init();
   State &s = st();
+  if (!s.ready && noalloc_used()) {
+    // Only gcvl_add_sed_noalloc has run, on the legacy default stream: wait
+    // for it and read its status word without the library's set-up, which
+    // allocates.
+    if (GCVL_CK(cudaStreamSynchronize(0))) noalloc_fold_status();
+    return s.err;
+  }
+  ensure_init();
   if (!s.ready) return s.err ? s.err : GCVL_ERR_CUDA;
   if (!GCVL_CK(cudaStreamSynchronize(s.stream))) return s.err;
   unsigned word = 0;
@@ -110,6 +117,7 @@ GCVL_EXPORT int gcvl_sync(void) {
     unsigned zero = 0;
     cudaMemcpy(s.d_status, &zero, 4, cudaMemcpyHostToDevice);
   }
+  noalloc_fold_status();
   return s.err;
 }
 

@@ -463,6 +463,9 @@ __global__ void __launch_bounds__(cta_threads<MODE>(), MODE == M_REDUCE ? (sizeo
     named_sync(1, TB_LB);  // carry ready / tile aggregate ready
     if (MODE != M_REDUCE && lane == 0 && tile > 0 && !first_head && !s_af)
       lb_publish(a.lb.word + tile, TS_INC, to_bits<T>(Op::apply(P, s_av)));
+    // the compute warps have waited for the tile (bounded): the issuing
+    // thread leaves only once it has landed
+    if (lane == 0 && !mbar_wait(&bar, 0, kDrainLimit)) atomicOr(a.status, DEV_TIMEOUT);
     return;
   }
 
@@ -494,7 +497,13 @@ __global__ void __launch_bounds__(cta_threads<MODE>(), MODE == M_REDUCE ? (sizeo
   {
     int it = 0;
     while (!mbar_try_wait(&bar, 0)) {
-      if (++it >= a.spin_limit) { atomicOr(a.status, DEV_TIMEOUT); break; }
+      if (++it >= a.spin_limit) {
+        // flagged; still let the tile land (bounded) before reading it, so
+        // that no copy into this CTA's shared memory outlives the CTA
+        atomicOr(a.status, DEV_TIMEOUT);
+        mbar_wait(&bar, 0, kDrainLimit);
+        break;
+      }
     }
   }
   const OffWin off{win, a.sv.off, sf, (SEG && W <= a.wmax) ? W : 0};
@@ -868,7 +877,7 @@ __device__ __forceinline__ void ring_arm(int t, unsigned long long *bar, unsigne
 // Bound on the waits that make sure a ring slot's load has landed before the
 // slot is armed again or the CTA exits.  They only spin after a load wait
 // already gave up (a timeout is flagged); otherwise the load is long done.
-constexpr int kRingDrain = 1 << 20;
+constexpr int kRingDrain = kDrainLimit;
 
 template <class Op, bool SEG>
 __global__ void __launch_bounds__(RTB, GCVL_RING_MINB)
@@ -1637,20 +1646,26 @@ GCVL_EXPORT unsigned pk1_lev_inplace(void) { return INPLACE_NONE; }
 // ============================================================================
 // add_sed for callers that cannot allocate device memory.
 //
-// Some callers of this library may not call cudaMalloc: code running while
-// a CUDA graph is being captured, embedders whose device memory is all
-// handed out by their own pool, or runtimes that forbid allocation after
-// start-up.  For them gcvl_add_sed_noalloc runs the same segmented +-scan as
-// add_sed but keeps its look-back scratch in the fixed array below instead
-// of a caller scratch vector or the library workspace, and it allocates
-// nothing: no cudaMalloc, cudaFree or other allocating call, and it does not
-// run the library's own first-use set-up (which allocates).
+// Some callers of this library may not call cudaMalloc: embedders whose
+// device memory is all handed out by their own pool or arena (a cudaMalloc
+// would fail, or take memory the pool already counts as its own), and
+// runtimes that forbid allocation after start-up because an allocation can
+// synchronise the device or fail at a time the caller cannot handle.  For
+// them gcvl_add_sed_noalloc runs the same segmented +-scan as add_sed but
+// keeps its look-back scratch in the fixed array below instead of a caller
+// scratch vector or the library workspace, and it allocates nothing: no
+// cudaMalloc, cudaFree or other allocating call, and it does not run the
+// library's own first-use set-up (which allocates).
 //
-// The array holds the scratch of at most GCVL_NOALLOC_MAX_N elements
-// (2^28; about 2 MB) and stays allocated on every GPU that loads the library until the
-// process exits.  All calls share it and it keeps the last call's contents;
-// each call clears the part that must start at zero.  Calls that overlap on
-// the GPU race on it: issue them on one stream, or order them.
+// The array holds the scratch of at most 2^28 elements: 2,097,664 bytes
+// (2.0 MiB), allocated on every GPU that loads the library until the process
+// exits.  All calls share it and it keeps the last call's contents; each call
+// clears the part that must start at zero.  Calls that overlap on the GPU
+// race on it: issue them on one stream, or order them.
+//
+// A bounded wait that gives up in these kernels sets a bit in a status word
+// of the same kind (g_noalloc_status); gcvl_sync reads and clears it like the
+// library's own status word and returns the timeout (error 3).
 // ============================================================================
 constexpr long kNoallocMaxN = 1L << 28;
 constexpr size_t kNoallocTiles = (size_t)(kNoallocMaxN / tile_elems<double>());  // smallest tiling
@@ -1658,10 +1673,37 @@ constexpr size_t kNoallocBytes = 512 + ((kNoallocTiles * 16 + 255) / 256) * 256;
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocBytes];
 static __device__ unsigned g_noalloc_status;
 
+static_assert(kNoallocBytes == 2097664, "the documented size of the fixed scratch array");
+
 // Device addresses of the array and of its status word, looked up once per
-// device (with that device current) on the first call made on it.
+// device (with that device current) on the first call made on it.  They are
+// kept until exit: a cudaDeviceReset on that device invalidates them, and no
+// call may follow one.
 static void *g_noalloc_ptr[128];
 static unsigned *g_noalloc_status_ptr[128];
+
+namespace gcvl {
+// Folds the no-allocation entry point's status word of the current device
+// into the library's error state and clears it.  Does nothing on a device
+// where that entry point has not run.  The caller has waited for the work.
+bool noalloc_used() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 128) return false;
+  return g_noalloc_status_ptr[dev] != nullptr;
+}
+void noalloc_fold_status() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 128 || !g_noalloc_status_ptr[dev]) return;
+  unsigned word = 0;
+  if (!GCVL_CK(cudaMemcpy(&word, g_noalloc_status_ptr[dev], 4, cudaMemcpyDeviceToHost))) return;
+  if (word & DEV_TIMEOUT)
+    set_error(GCVL_ERR_TIMEOUT, "a bounded device wait gave up in gcvl_add_sed_noalloc (status 0x%x)", word);
+  if (word) {
+    unsigned zero = 0;
+    GCVL_CK(cudaMemcpy(g_noalloc_status_ptr[dev], &zero, 4, cudaMemcpyHostToDevice));
+  }
+}
+}  // namespace gcvl
 
 GCVL_EXPORT int gcvl_add_sed_noalloc(vec_p d, vec_p s, vec_p sd, int n, int m) {
   using namespace gcvl;
@@ -1721,8 +1763,10 @@ GCVL_EXPORT int gcvl_add_sed_noalloc(vec_p d, vec_p s, vec_p sd, int n, int m) {
     if (seg) k_scan<AddD, M_SCAN, true><<<tiles, Tiling<double>::BLOCK, 0, strm>>>(a);
     else k_scan<AddD, M_SCAN, false><<<tiles, Tiling<double>::BLOCK, 0, strm>>>(a);
   }
+  // launch_check clears the launch error it records, so read it first
+  const cudaError_t launched = cudaPeekAtLastError();
   launch_check("gcvl_add_sed_noalloc");
-  return cudaPeekAtLastError() == cudaSuccess ? GCVL_OK : GCVL_ERR_CUDA;
+  return launched == cudaSuccess ? GCVL_OK : GCVL_ERR_CUDA;
 }
 
 GCVL_EXPORT long gcvl_add_sed_noalloc_max_n(void) { return kNoallocMaxN; }

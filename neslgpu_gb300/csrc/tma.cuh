@@ -55,6 +55,9 @@ __device__ __forceinline__ void bulk_load_1d(void *dst, const void *src, unsigne
 __device__ __forceinline__ void mbar_arrive(unsigned long long *bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
 }
+// Iteration limit of the waits that let a CTA's own bulk copies land before
+// it reads or leaves their shared memory, after a shorter wait gave up.
+constexpr int kDrainLimit = 1 << 20;
 // Bounded wait for the completion of phase `parity`; false on timeout.
 __device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned parity, int limit) {
   int it = 0;
