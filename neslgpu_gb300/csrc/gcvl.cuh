@@ -36,7 +36,7 @@ struct State {
   size_t work_bytes = 0;            //   passes a NULL scratch vector
   void *stage = nullptr;            // staging buffer for overlapping mov_fov
   size_t stage_bytes = 0;
-  uint64_t rand48 = 0x1234ABCD330EULL;  // lrand48 state (POSIX initial value)
+  uint64_t rand48 = 0;               // lrand48 state (glibc starts unseeded draws from 0)
   int spin_limit = 1 << 22;         // bounded-wait iteration limit
   int err = 0;
   char msg[256] = {0};

@@ -244,13 +244,15 @@ GCVL_EXPORT int gcvl_selftest_timeout(int limit) {
 
 // =================================================== CVL facility functions
 // CVL_init (cvl.h:121-123, CUDA build): records the fused super-op library
-// named by vinterp's -l flag and brings the device up.
+// named by vinterp's -l flag and brings the device up.  The serial CVL_init
+// calls rnd_foz(0) (facilt.c:316-319), which on Linux is srandom(0) and leaves
+// lrand48 unseeded: RAND then draws glibc's unseeded stream, from state 0.
 GCVL_EXPORT void CVL_init(char *lib) {
   if (lib) {
     strncpy(st().fused_lib, lib, sizeof(st().fused_lib) - 1);
   }
   ensure_init();
-  st().rand48 = 0x1234ABCD330EULL;
+  st().rand48 = 0;
 }
 
 // Timers (facilt.c:43-99).  tgt_fos drains the library stream first so that

@@ -152,8 +152,10 @@ EXPORT void ocvl_cpy_wus(vec_p d, vec_p s, int n, int m, vec_p scr) {
 
 /* ---- RAND: rnd_wuz (elwise.c:211-236) draws (int)lrand48() % s[i] in
  * order.  The oracle keeps its own 48-bit lrand48 state so that runs do not
- * depend on libc state; rnd_foz seeds it as srand48(seed) does. ---------- */
-static uint64_t g_rand48 = 0x1234ABCD330EULL; /* POSIX initial state */
+ * depend on libc state; rnd_foz seeds it as srand48(seed) does.  Before any
+ * seeding the state is 0: glibc's lrand48, which the serial CVL calls on
+ * Linux, starts there (POSIX leaves the unseeded state to the C library). */
+static uint64_t g_rand48 = 0;
 EXPORT void ocvl_rnd_foz(int seed) {
   g_rand48 = (((uint64_t)(uint32_t)seed) << 16 | 0x330EULL) & 0xFFFFFFFFFFFFULL;
 }
@@ -412,6 +414,20 @@ EXPORT void ocvl_len_fos(vec_p l, vec_p sd, int n, int m, vec_p scr) {
  * the VCODE interpreter when it runs on the oracle. */
 EXPORT vec_p ocvl_alo_foz(int size) { return malloc((size_t)(size > 0 ? size : 1) * UNIT); }
 EXPORT void ocvl_fre_fov(vec_p p) { free(p); }
+/* mov_fov (facilt.c:160-183): move `size` units that may overlap, one unit
+ * at a time, front to back when moving down and back to front when moving
+ * up, so every unit is read before it is overwritten. */
+EXPORT void ocvl_mov_fov(vec_p d, vec_p s, int size, vec_p scr) {
+  uint64_t *dst = (uint64_t *)d;
+  const uint64_t *src = (const uint64_t *)s;
+  (void)scr;
+  if (dst == src) return;
+  if (dst < src) {
+    for (int i = 0; i < size; i++) dst[i] = src[i];
+  } else {
+    for (int i = size - 1; i >= 0; i--) dst[i] = src[i];
+  }
+}
 #define XFER(L, T)                                                                      \
   EXPORT void ocvl_v2c_fu##L(void *d, vec_p s, int len, vec_p scr) {                    \
     (void)scr; if (len > 0) memcpy(d, s, (size_t)len * sizeof(T));                      \

@@ -71,6 +71,40 @@ def seg_abs_total(x, lengths):
     return c[ends] - c[starts]
 
 
+def sum_err_over_tol(got, want, x, lengths, kind, chunk=1 << 24):
+    """max over elements of |got - want| / (1e-12 * max(|want|, S)) for a
+    segmented float64 +-scan (kind "scan": S = sum of |x| before the element
+    in its segment) or +-reduction ("reduce": S = sum of |x| over the
+    segment), computed over groups of whole segments of about `chunk`
+    elements so that vectors of 2^28 elements need little extra memory.
+    A result passes when the value is <= 1."""
+    x = np.asarray(x, dtype=np.float64)
+    lengths = np.asarray(lengths, dtype=np.int64)
+    ends = np.cumsum(lengths)
+    starts = ends - lengths
+    worst = 0.0
+    a = 0
+    m = len(lengths)
+    while a < m:
+        b = max(a + 1, int(np.searchsorted(ends, starts[a] + chunk, side="right")))
+        b = min(b, m)
+        e0, e1 = int(starts[a]), int(ends[b - 1])
+        ln = lengths[a:b]
+        if kind == "scan":
+            S = seg_abs_prefix(x[e0:e1], ln)
+            g, w = got[e0:e1], want[e0:e1]
+        else:
+            S = seg_abs_total(x[e0:e1], ln)
+            g, w = got[a:b], want[a:b]
+        if len(w):
+            tol = SUM_RTOL * np.maximum(np.abs(w), S) + 1e-300
+            err = np.abs(g - w)
+            same = (g == w) | (np.isnan(g) & np.isnan(w))
+            worst = max(worst, float(np.max(np.where(same, 0.0, err / tol))))
+        a = b
+    return worst
+
+
 SCAN_OPS = [("add", "z"), ("add", "d"), ("mul", "z"), ("mul", "d"), ("min", "z"), ("min", "d"),
             ("max", "z"), ("max", "d"), ("and", "b"), ("and", "z"), ("ior", "b"), ("ior", "z"),
             ("xor", "b"), ("xor", "z")]
