@@ -20,9 +20,12 @@ Printed as one JSON line (rank 0).  Besides the headline it carries:
                   v2c_fud x2)
   cpu_baseline -- the CPU oracle (plain-C restatement of the serial CVL)
                   on one host core over the same workload
+  parity       -- the timed GPU results against that CPU run under the
+                  float64 rule |gpu - cpu| <= 1e-12 * max(|cpu|, S)
   primitives   -- Gelem/s and roofline fraction of the other CVL primitives
                   at 2^28 elements (int32 unless named)
-  clocks       -- nvidia-smi samples taken during the timed region
+  clocks       -- SM clock and throttle reasons sampled (NVML, every
+                  millisecond) during the timed region
 
 ``--impl reference`` times the CPU implementation of the same step (the
 oracle restatement of the serial CVL; the reference sources are not on this
@@ -71,17 +74,61 @@ def segment_lengths(n):
 
 
 class Clocks:
-    """nvidia-smi sampling during the timed region."""
+    """SM clock and throttle reasons sampled during the timed region.
+
+    NVML (libnvidia-ml, read-only queries) is polled every millisecond from a
+    thread, so that a timed region of a few tens of milliseconds still holds
+    tens of samples; where NVML cannot be loaded, nvidia-smi's own 100 ms
+    loop stands in."""
 
     Q = ("timestamp,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
          "clocks_event_reasons.sw_power_cap")
+    # nvmlClocksEventReason* bits (nvml.h)
+    REASONS = {0x8: "hw_slowdown", 0x40: "hw_thermal_slowdown", 0x20: "sw_thermal_slowdown",
+               0x4: "sw_power_cap"}
 
-    def __init__(self, device):
+    def __init__(self, device, period_s=0.001):
         self.device = device
+        self.period = period_s
         self.proc = None
+        self.thread = None
+        self.samples = []  # (host time, sm MHz, max MHz, reason bits)
+
+    def _nvml(self):
+        try:
+            nv = C.CDLL("libnvidia-ml.so.1")
+        except OSError:
+            return None
+        if nv.nvmlInit_v2() != 0:
+            return None
+        count = C.c_uint(0)
+        if nv.nvmlDeviceGetCount_v2(C.byref(count)) != 0 or count.value == 0:
+            return None
+        h = C.c_void_p()
+        idx = self.device if count.value > self.device else 0
+        if nv.nvmlDeviceGetHandleByIndex_v2(C.c_uint(idx), C.byref(h)) != 0:
+            return None
+        return nv, h
+
+    def _poll(self, nv, h):
+        clk, mx, rs = C.c_uint(0), C.c_uint(0), C.c_ulonglong(0)
+        nv.nvmlDeviceGetMaxClockInfo(h, 1, C.byref(mx))  # NVML_CLOCK_SM
+        get_reasons = getattr(nv, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            nv.nvmlDeviceGetCurrentClocksThrottleReasons
+        while not self.stop:
+            t = time.time()
+            if nv.nvmlDeviceGetClockInfo(h, 1, C.byref(clk)) == 0 and get_reasons(h, C.byref(rs)) == 0:
+                self.samples.append((t, float(clk.value), float(mx.value), int(rs.value)))
+            time.sleep(self.period)
 
     def __enter__(self):
+        self.stop = False
+        got = self._nvml()
+        if got is not None:
+            self.thread = threading.Thread(target=self._poll, args=got, daemon=True)
+            self.thread.start()
+            return self
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
@@ -92,6 +139,9 @@ class Clocks:
         return self
 
     def __exit__(self, *a):
+        self.stop = True
+        if self.thread:
+            self.thread.join(timeout=5)
         self.out = ""
         if self.proc:
             self.proc.terminate()
@@ -101,13 +151,10 @@ class Clocks:
                 self.proc.kill()
                 self.out, _ = self.proc.communicate()
 
-    def summary(self, t0=None, t1=None):
-        """Median SM clock and active throttle reasons over the samples whose
-        timestamps fall inside [t0, t1] (host wall-clock seconds)."""
+    def _smi_samples(self):
         import datetime as dt
-        sm, mx, reasons = [], 0.0, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        total = 0
+        bits = {v: k for k, v in self.REASONS.items()}
         for line in (getattr(self, "out", "") or "").splitlines():
             f = [x.strip() for x in line.split(",")]
             if len(f) < 8:
@@ -117,16 +164,53 @@ class Clocks:
                 clk, cmax = float(f[1]), float(f[2])
             except ValueError:
                 continue
-            total += 1
-            if t0 is not None and not (t0 - 0.05 <= ts <= t1 + 0.05):
+            rs = sum(bits[nm] for nm, v in zip(names, f[4:8]) if v.lower() == "active")
+            yield ts, clk, cmax, rs
+
+    def summary(self, t0=None, t1=None):
+        """Median SM clock and active throttle reasons over the samples whose
+        timestamps fall inside [t0, t1] (host wall-clock seconds)."""
+        samples = self.samples if self.thread else list(self._smi_samples())
+        sm, mx, reasons = [], 0.0, set()
+        for ts, clk, cmax, rs in samples:
+            if t0 is not None and not (t0 - 0.002 <= ts <= t1 + 0.002):
                 continue
             sm.append(clk)
             mx = max(mx, cmax)
-            for nm, v in zip(names, f[4:8]):
-                if v.lower() == "active":
-                    reasons.add(nm)
+            reasons.update(nm for b, nm in self.REASONS.items() if rs & b)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None,
-                "reasons": sorted(reasons), "samples_in_window": len(sm), "samples": total}
+                "reasons": sorted(reasons), "samples_in_window": len(sm), "samples": len(samples),
+                "source": "nvml, 1 ms" if self.thread else "nvidia-smi, 100 ms"}
+
+
+def sum_err_over_tol(got, want, x, lens, kind, chunk=1 << 24):
+    """max |got - want| / (1e-12 * max(|want|, S)) over a segmented float64
+    +-scan (S = sum of |x| before the element in its segment) or
+    +-reduction (S = sum of |x| over the segment), over groups of whole
+    segments of about `chunk` elements."""
+    lens = np.asarray(lens, dtype=np.int64)
+    ends = np.cumsum(lens)
+    starts = ends - lens
+    worst, a, m = 0.0, 0, len(lens)
+    while a < m:
+        b = min(m, max(a + 1, int(np.searchsorted(ends, starts[a] + chunk, side="right"))))
+        e0, e1 = int(starts[a]), int(ends[b - 1])
+        ln = lens[a:b]
+        ax = np.abs(x[e0:e1])
+        cs = np.concatenate([[0.0], np.cumsum(ax)])
+        ls = np.cumsum(ln) - ln
+        if kind == "scan":
+            S = cs[np.arange(e1 - e0)] - cs[np.repeat(ls, ln)]
+            g, w = got[e0:e1], want[e0:e1]
+        else:
+            S = cs[ls + ln] - cs[ls]
+            g, w = got[a:b], want[a:b]
+        if len(w):
+            tol = 1e-12 * np.maximum(np.abs(w), S) + 1e-300
+            same = (g == w) | (np.isnan(g) & np.isnan(w))
+            worst = max(worst, float(np.max(np.where(same, 0.0, np.abs(g - w) / tol))))
+        a = b
+    return worst
 
 
 def dist():
@@ -697,7 +781,7 @@ def gpu_arm(a):
                "sequential": {"value": round(world * 2 * n / dt_seq / 1e9, 3), "ms_per_step": round(dt_seq * 1e3, 3),
                               "api": "c2v_fud, add_sed, add_red, v2c_fud x2 on the whole vector"}}
 
-    cpu = None
+    cpu = parity = None
     if rank == 0 and world == 1 and not a.no_cpu:
         xh = np.empty(n)
         c.v2c_fud(xh.ctypes.data, x, n, None)
@@ -710,8 +794,13 @@ def gpu_arm(a):
         c.v2c_fud(gs.ctypes.data, ys, n, None)
         gr = np.empty(m)
         c.v2c_fud(gr.ctypes.data, yr, m, None)
-        cpu["max_rel_diff_scan"] = float(np.max(np.abs(gs - scan) / np.maximum(np.abs(scan), 1.0)))
-        cpu["max_rel_diff_reduce"] = float(np.max(np.abs(gr - red) / np.maximum(np.abs(red), 1.0)))
+        e_scan = sum_err_over_tol(gs, scan, xh, lens, "scan")
+        e_red = sum_err_over_tol(gr, red, xh, lens, "reduce")
+        parity = {"rule": "|gpu - cpu| <= 1e-12 * max(|cpu|, S), S = sum of |x| over the same prefix "
+                          "(add_sed) or segment (add_red); err/tol <= 1 passes",
+                  "max_err_over_tol": {"add_sed": e_scan, "add_red": e_red},
+                  "ok": bool(e_scan <= 1.0 and e_red <= 1.0),
+                  "against": "the oracle (CPU restatement of the serial CVL) on the same values"}
 
     prims = batched = dispatch = vinterp = None
     if not a.no_suite and rank == 0:
@@ -731,7 +820,8 @@ def gpu_arm(a):
                        "n": n, "m": m, "elements_per_step": 2 * n,
                        "l2": "inputs larger than L2 (2 GiB per vector), no flush",
                        "parallelism": f"{world} independent replicas"},
-            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
+            "roofline": roofline, "cpu_baseline": cpu, "parity": parity, "e2e": e2e,
+            "gpu_launches": int(launches),
             "clocks": clk.summary(w0, w1), "primitives": prims, "batched": batched, "dispatch": dispatch,
             "vinterp": vinterp,
         }
@@ -752,7 +842,7 @@ def reference_arm(a):
     cores = os.cpu_count() or 1
     x = W.float64_normal(W.rng(SEED), n)
     times = []
-    for _ in range(a.warmup if a.warmup < 2 else 1):
+    for _ in range(a.warmup):
         cpu_baseline_port(x, lens, threads=cores)
     for _ in range(a.steps):
         t, _, _ = cpu_baseline_port(x, lens, threads=cores)
@@ -797,7 +887,6 @@ def main():
     a = ap.parse_args()
     a.warmup = max(a.warmup, 3) if a.impl == "gb300" else a.warmup
     if a.impl == "reference":
-        a.steps = min(a.steps, 5)
         reference_arm(a)
     elif a.suite_only:
         g = Gpu()
