@@ -66,7 +66,7 @@ def build_library(verbose: bool = False, force: bool = False) -> Path:
             if verbose and err:
                 print(err, file=sys.stderr)
     if force or jobs or _stale(LIB, objs):
-        cmd = [nvcc(), *ARCH, "-shared", "-o", str(LIB), *map(str, objs)]
+        cmd = [nvcc(), *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-ldl"]
         run(cmd)
     return LIB
 

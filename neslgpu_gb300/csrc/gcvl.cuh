@@ -40,7 +40,8 @@ struct State {
   int spin_limit = 1 << 22;         // bounded-wait iteration limit
   int err = 0;
   char msg[256] = {0};
-  char fused_lib[1024] = {0};
+  char fused_lib[1024] = {0};       // fused library named by CVL_init
+  bool fused_init_done = false;     // its init() has been given the heap
 };
 State &st();
 void ensure_init();

@@ -11,6 +11,7 @@
 #include <stdio.h>
 #include <stdlib.h>
 #include <time.h>
+#include <dlfcn.h>
 
 namespace gcvl {
 
@@ -250,6 +251,7 @@ GCVL_EXPORT int gcvl_selftest_timeout(int limit) {
 GCVL_EXPORT void CVL_init(char *lib) {
   if (lib) {
     strncpy(st().fused_lib, lib, sizeof(st().fused_lib) - 1);
+    st().fused_init_done = false;
   }
   ensure_init();
   st().rand48 = 0;
@@ -283,7 +285,25 @@ GCVL_EXPORT int siz_fos(int n, int m) {
 }
 
 // Memory (facilt.c:148-234).  alo_foz returns NULL when the device is out
-// of memory, as the serial CVL returns NULL from malloc.
+// of memory, as the serial CVL returns NULL from malloc.  The first
+// allocation after CVL_init named a fused library passes its base to that
+// library's init(), as the reference's CUDA CVL does with its heap
+// (nesl/cvl/cuda/facilities.c:206-221); a library that cannot be opened or
+// has no init makes that allocation fail, as there.
+static bool call_fused_init(void *base) {
+  State &s = st();
+  void *h = dlopen(s.fused_lib, RTLD_NOW);
+  if (!h) { set_error(GCVL_ERR_ARG, "alo_foz: cannot load fused library %s: %s", s.fused_lib, dlerror()); return false; }
+  void (*init_fn)(void *) = (void (*)(void *))dlsym(h, "init");
+  if (!init_fn) {
+    set_error(GCVL_ERR_ARG, "alo_foz: fused library %s has no init", s.fused_lib);
+    dlclose(h);
+    return false;
+  }
+  init_fn(base);
+  dlclose(h);
+  return true;
+}
 GCVL_EXPORT vec_p alo_foz(int size) {
   ensure_init();
   if (size < 0) { set_error(GCVL_ERR_ARG, "alo_foz: negative size %d", size); return nullptr; }
@@ -294,6 +314,14 @@ GCVL_EXPORT vec_p alo_foz(int size) {
     cudaGetLastError();
     set_error(GCVL_ERR_NOMEM, "alo_foz(%d units): %s", size, cudaGetErrorString(e));
     return nullptr;
+  }
+  State &s = st();
+  if (s.fused_lib[0] && !s.fused_init_done) {
+    s.fused_init_done = true;
+    if (!call_fused_init(p)) {
+      cudaFree(p);
+      return nullptr;
+    }
   }
   return p;
 }

@@ -20,6 +20,18 @@ and exposes them to the VCODE interpreter (``vcode.Interpreter(...,
 fused=lib)``), which runs ``FUSED k`` like vinterp runs a fused library's
 op k: arguments from the stack, result length that of the first argument
 (the element count of a segment descriptor argument).
+
+The generated library is also a fused library for the reference's own
+interpreter: vinterp ``dlopen``s the library named by its ``-l`` flag and
+takes the operation table ``vops[]`` and the function table ``cvl_funs[]``
+from it (nesl/vcode/fusion.c:18-42); the reference's CUDA CVL also calls the
+library's ``init`` with its heap base (nesl/cvl/cuda/facilities.c:206-221).
+All three are exported, with the layouts of ``vopdes_t`` and
+``cvl_triple_t`` (nesl/vcode/vcode.h:73-100) and entries made by the fusion
+compiler's rules (nesl/fusion/super-op-gen.sml:346-440).  The entries carry
+vinterp's token numbers: pass its ``y.tab.h`` as ``build_library(...,
+ytab=path)``; without one, the numbers bison -y gives the grammar
+(nesl/vcode/grammar.yy:43-96, 258 + declaration index) are used.
 """
 from __future__ import annotations
 
@@ -202,6 +214,93 @@ def _expr(n: Node) -> str:
     return f"gcvl::f_{stem}_{sfx}::f({', '.join(_expr(a) for a in n.args)})"
 
 
+# vinterp's enumerations (nesl/vcode/vcode.h:12-13, 38-48, 58-70) and the
+# bison -y token numbers of the two opcodes a fused table names
+# (nesl/vcode/grammar.yy: MAKE_SEGDES is token 66 and FUSED token 112 in
+# declaration order, numbered from 258)
+VTYPE = {"BOOL": 3, "INT": 4, "FLOAT": 5, "SEGDES": 6}
+AGREE1, COMPAT1 = 0x1, 0x20
+CVL_DESC_SEGOP, CVL_DESC_NOT_SUPPORTED = 44, 56
+BISON_FUSED, BISON_MAKE_SEGDES = 258 + 112, 258 + 66
+MAX_ARGS = 40
+
+
+def _vinterp_tables(ops: list[FusedOp]) -> list[str]:
+    """vops[], cvl_funs[] and init() for vinterp's fused-library loader,
+    indexed by super-op number (numbers missing from the definitions get a
+    NotSupported entry)."""
+    lines = [
+        "// ---- the fused-library interface of vinterp (fusion.c:18-42) ----",
+        "#ifdef GCVL_VINTERP_YTAB",
+        "#include GCVL_VINTERP_YTAB",
+        "#endif",
+        "#ifndef FUSED",
+        f"#define FUSED {BISON_FUSED}",
+        "#endif",
+        "#ifndef MAKE_SEGDES",
+        f"#define MAKE_SEGDES {BISON_MAKE_SEGDES}",
+        "#endif",
+        "struct gcvl_vopdes {  // vopdes_t",
+        "  int vop; const char *vopname; int arg_num; int result_num;",
+        f"  int arg_type[{MAX_ARGS}]; unsigned arg_len[{MAX_ARGS}]; int result_type[3]; unsigned result_len[3];",
+        f"  int arg_for_scratch[{MAX_ARGS}]; int cvl_desc;",
+        "};",
+        "struct gcvl_funct { void (*function)(); int (*scratch_function)(); unsigned (*inplace_function)(); };",
+        "struct gcvl_triple { gcvl_funct cvl_int, cvl_float, cvl_boolean; };  // cvl_triple_t",
+        "// vec_p is a device pointer in this library: the heap base is not needed",
+        "static void *g_heap_base = 0;",
+        'extern "C" __attribute__((visibility("default"))) void init(void *mem) { g_heap_base = mem; }',
+        'extern "C" __attribute__((visibility("default"))) void fused_unsupported(void) {}',
+        'extern "C" __attribute__((visibility("default"))) int fused_unsupported_scratch(void) { return 0; }',
+        'extern "C" __attribute__((visibility("default"))) unsigned fused_unsupported_inplace(void) { return 0; }',
+    ]
+    by = {o.number: o for o in ops}
+    top = max(by) + 1 if by else 0
+    vops, funs = [], []
+    for k in range(top):
+        o = by.get(k)
+        if o is None:
+            vops.append(f'  {{FUSED + {k}, "unsupported", 0, 0, {{0}}, {{0}}, {{0}}, {{0}}, {{0}}, '
+                        f'{CVL_DESC_NOT_SUPPORTED}}},')
+            f = ("fused_unsupported",) * 3
+        else:
+            arity = len(o.params)
+            if arity > MAX_ARGS:
+                raise FcodeError(f"OP{k}: {arity} arguments, vinterp takes at most {MAX_ARGS}")
+            types = ", ".join(str(VTYPE[t]) for _, t in o.params) or "0"
+            seg_result = o.result == "SEGDES"
+            vop = "MAKE_SEGDES" if seg_result else f"FUSED + {k}"
+            rlen = COMPAT1 if o.params and o.params[0][1] == "SEGDES" else AGREE1
+            desc = CVL_DESC_SEGOP if seg_result else arity
+            vops.append(f'  {{{vop}, "fused{k}", {arity}, 1, {{{types}}}, {{0}}, {{{VTYPE[o.result]}}}, '
+                        f'{{{rlen}}}, {{1}}, {desc}}},')
+            f = (f"fused{k}", f"fused{k}_scratch", f"fused{k}_inplace")
+        slot = f"{{(void (*)()){f[0]}, (int (*)()){f[1]}, (unsigned (*)()){f[2]}}}"
+        funs.append(f"  {{{slot}, {slot}, {slot}}},")
+    lines.append(f'extern "C" __attribute__((visibility("default"))) gcvl_vopdes vops[{max(top, 1)}] = {{')
+    lines += vops or ['  {0, "none", 0, 0, {0}, {0}, {0}, {0}, {0}, ' + f"{CVL_DESC_NOT_SUPPORTED}}},"]
+    lines.append("};")
+    lines.append(f'extern "C" __attribute__((visibility("default"))) gcvl_triple cvl_funs[{max(top, 1)}] = {{')
+    unsup = "{(void (*)())fused_unsupported, (int (*)())fused_unsupported_scratch, " \
+            "(unsigned (*)())fused_unsupported_inplace}"
+    lines += funs or [f"  {{{unsup}, {unsup}, {unsup}}},"]
+    lines.append("};")
+    return lines
+
+
+def _inplace_flag(o: FusedOp) -> int:
+    """INPLACE_i for the first argument i (from 1) that is not a segment
+    descriptor, none for a descriptor result (super-op-gen.sml:355-366).
+    Every generated kernel reads all of an element's inputs before writing
+    it, so any such argument may share the result's memory."""
+    if o.result == "SEGDES":
+        return 0
+    for i, (_, t) in enumerate(o.params, start=1):
+        if t != "SEGDES":
+            return 1 << (i - 1)
+    return 0
+
+
 def emit_cuda(ops: list[FusedOp]) -> str:
     lines = [
         "// generated by neslgpu_gb300/fcode.py from fused super-op definitions",
@@ -250,15 +349,19 @@ def emit_cuda(ops: list[FusedOp]) -> str:
         lines.append(f'extern "C" __attribute__((visibility("default"))) int fused{k}_scratch(int len) '
                      "{ (void)len; return 0; }")
         lines.append(f'extern "C" __attribute__((visibility("default"))) unsigned fused{k}_inplace(void) '
-                     "{ return 0; }")
+                     f"{{ return {_inplace_flag(o)}u; }}")
+    lines += _vinterp_tables(ops)
     return "\n".join(lines) + "\n"
 
 
-def build_library(ops: list[FusedOp], out_dir: Path | None = None) -> Path:
+def build_library(ops: list[FusedOp], out_dir: Path | None = None, ytab: Path | None = None) -> Path:
     """nvcc the generated source for sm_103a into a shared library (cached
-    by the source's hash); returns its path."""
+    by the source's hash); returns its path.  ytab: the y.tab.h of the
+    vinterp build that will load the library (its token numbers go into
+    vops[])."""
     src = emit_cuda(ops)
-    h = hashlib.sha256(src.encode()).hexdigest()[:16]
+    key = src + (Path(ytab).read_text() if ytab else "")
+    h = hashlib.sha256(key.encode()).hexdigest()[:16]
     d = Path(out_dir or CACHE)
     d.mkdir(parents=True, exist_ok=True)
     so = d / f"fused_{h}.so"
@@ -270,6 +373,7 @@ def build_library(ops: list[FusedOp], out_dir: Path | None = None) -> Path:
     # linked against the library for its stream (gcvl_get_stream)
     cmd = ["nvcc", "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17", "-shared",
            "-Xcompiler", "-fPIC", f"-I{CSRC}", f"-I{INCLUDE}", "-o", str(tmp), str(cu),
+           *([f'-DGCVL_VINTERP_YTAB="{Path(ytab).resolve()}"'] if ytab else []),
            f"-L{PKG}", "-lcvl_gb300", "-Xlinker", "-rpath", "-Xlinker", str(PKG)]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
