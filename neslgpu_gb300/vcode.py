@@ -27,6 +27,7 @@ library or, for the parity tests and the CPU baseline, the oracle.
 """
 from __future__ import annotations
 
+import io
 import re
 import sys
 import time
@@ -76,6 +77,10 @@ class VcodeError(RuntimeError):
     pass
 
 
+# instructions a trace leaves out: host I/O and process control
+_UNTRACED = {"READ", "WRITE", "FREAD", "FWRITE", "FOPEN", "FCLOSE", "FREAD_CHAR", "SPAWN"}
+
+
 # --------------------------------------------------------------- parse ---
 @dataclass
 class Ins:
@@ -92,12 +97,16 @@ _TOKEN = re.compile(r"\{[^}]*\}|\(|\)|\"[^\"]*\"|[^\s(){}\"]+")
 def parse(text: str) -> tuple[list[Ins], dict[str, int], str]:
     """VCODE text -> (instructions, function entry points, first function).
     Grammar after nesl/vcode/grammar.yy: FUNC name [I types O types]
-    statements RET; comments in braces."""
+    statements RET; comments in braces.  Comments and strings may run over
+    several lines (nesl/vcode/tokens.ll:33-34)."""
     toks = []
-    for lineno, line in enumerate(text.splitlines(), 1):
-        for t in _TOKEN.findall(line):
-            if not t.startswith("{"):
-                toks.append((t, lineno))
+    lineno, at = 1, 0
+    for mt in _TOKEN.finditer(text):
+        lineno += text.count("\n", at, mt.start())
+        at = mt.start()
+        t = mt.group(0)
+        if not t.startswith("{"):
+            toks.append((t, lineno))
     prog: list[Ins] = []
     funcs: dict[str, int] = {}
     first = None
@@ -147,7 +156,12 @@ def parse(text: str) -> tuple[list[Ins], dict[str, int], str]:
         elif t == "CONST":
             typ = toks[i][0]
             i += 1
-            if peek() == "(":
+            if typ == "CHAR" and peek() is not None and peek().startswith('"'):
+                # a string: the codes of the characters between the quotes,
+                # taken as they are (constant.c:124-155)
+                prog.append(Ins("CONSTV", typ, [ord(ch) for ch in toks[i][0][1:-1]], None, ln))
+                i += 1
+            elif peek() == "(":
                 i += 1
                 vals = []
                 while peek() != ")":
@@ -261,13 +275,34 @@ class _VStream:
         self.buf = ""
 
     def _fill(self) -> bool:
-        chunk = self.f.read(1 << 16)
+        # what is there now, up to 64 KB: a pipe or terminal must not wait
+        # for a full block
+        raw = getattr(self.f, "buffer", None)
+        if raw is not None and hasattr(raw, "read1"):
+            chunk = raw.read1(1 << 16).decode("latin-1")
+        else:
+            chunk = self.f.read(1 << 16)
         self.buf += chunk
         return bool(chunk)
 
     def write(self, text: str):
         self.f.write(text)
         self.f.flush()
+
+    def read_chars(self, max_char: int, delims: set):
+        """Characters up to a delimiter (consumed, not returned), the end of
+        the file or max_char of them: (codes, stop) with stop -2 at
+        max_char, -1 at the end, else the delimiter (io.c:1249-1290)."""
+        out = []
+        while len(out) < max_char:
+            if not self.buf and not self._fill():
+                return out, -1
+            c = ord(self.buf[0])
+            self.buf = self.buf[1:]
+            if c in delims:
+                return out, c
+            out.append(c)
+        return out, -2
 
     def read_vector(self, typ: str):
         """(values, None) or (None, error message)."""
@@ -333,6 +368,10 @@ class Interpreter:
         self._fn = {}
         # VCODE file descriptors: 0, 1, 2 are the standard streams
         self.files: dict[int, _VStream] = {0: _VStream(sys.stdin), 1: _VStream(sys.stdout), 2: _VStream(sys.stderr)}
+        # trace(op, typ, consumed, produced): called after every vector
+        # instruction other than I/O with (kind, segment count or None,
+        # values) triples of the stack entries it took and left; None: off
+        self.trace = None
 
     # -- memory
     def fn(self, name):
@@ -510,9 +549,37 @@ class Interpreter:
                 st.append(v)
             elif op == "EXIT":
                 break
+            elif self.trace is not None and op not in _UNTRACED:
+                self._traced_op(ins)
             else:
                 self._vector_op(ins)
         return self.stack
+
+    def _traced_op(self, ins, depth: int = 8):
+        """_vector_op, reporting the values it consumed and produced to
+        self.trace (an instruction takes and leaves entries at the top of
+        the stack only, so the first position whose entry changed splits
+        the two).  The top entries are held by one more reference during
+        the instruction, so none is updated in place and returned as its
+        own result."""
+        st = self.stack
+        old = list(st)
+        top = old[max(0, len(old) - depth):]
+        snap = [(v.kind, v.seg_len, self.to_host(v)) for v in top]
+        for v in top:
+            v.ref += 1
+        self._vector_op(ins)
+        for v in top:
+            self.drop(v)
+        p = 0
+        while p < len(old) and p < len(st) and st[p] is old[p]:
+            p += 1
+        taken = len(old) - p
+        if taken > len(top):
+            raise VcodeError(f"line {ins.line}: {ins.op} took more than {depth} stack entries")
+        consumed = snap[len(snap) - taken:] if taken else []
+        produced = [(v.kind, v.seg_len, self.to_host(v)) for v in st[p:]]
+        self.trace(ins.op, ins.typ, consumed, produced)
 
     def _const(self, ins):
         t = ins.typ
@@ -697,7 +764,7 @@ class Interpreter:
             s = st[-1]
             self.fn("rnd_foz")(self.scalar_int(s))
             self._finish(1, [self.const_scalar("B", True)])
-        elif op in ("READ", "WRITE", "FREAD", "FWRITE", "FOPEN", "FCLOSE"):
+        elif op in ("READ", "WRITE", "FREAD", "FWRITE", "FOPEN", "FCLOSE", "FREAD_CHAR", "SPAWN"):
             self._io(ins)
         else:
             raise VcodeError(f"line {ins.line}: {op} is not supported")
@@ -780,7 +847,9 @@ class Interpreter:
             self.drop(nv)
             fd, err = -1, None
             try:
-                f = open(name, {1: "r", 2: "w", 3: "a"}[mode])
+                # bytes in and out as they are (vinterp's stdio streams): no
+                # newline translation, one character per byte
+                f = open(name, {1: "r", 2: "w", 3: "a"}[mode], encoding="latin-1", newline="")
                 free = [k for k in range(3, MAX_FILES) if k not in self.files]
                 if free:
                     fd = free[0]
@@ -792,6 +861,29 @@ class Interpreter:
                 err = e.strerror or str(e)
             st.append(self.from_host("I", [fd]))
             self._push_io_status(err)
+        elif op == "FREAD_CHAR":
+            # fd, the most characters to read (negative: no limit) and a
+            # string of delimiters -> the characters, the stop status, the
+            # error string and the success flag (io.c:1134-1300)
+            fd, err = self._fd_from_stack(ins)
+            mv, dv = st.pop(), st.pop()
+            if fd is None or fd < 0:
+                self.drop(mv)
+                self.drop(dv)
+                st.append(self.new("I", 0))
+                st.append(self.new("I", 0))
+                self._push_io_status(err or "illegal VCODE file descriptor in FREAD")
+            else:
+                max_char = self.scalar_int(mv)
+                delims = set(self.to_host(dv).tolist())
+                self.drop(mv)
+                self.drop(dv)
+                codes, stop = self.files[fd].read_chars(max_char if max_char >= 0 else 1 << 30, delims)
+                st.append(self.from_host("I", codes))
+                st.append(self.from_host("I", [stop]))
+                self._push_io_status(None)
+        elif op == "SPAWN":
+            self._spawn(ins)
         elif op == "FCLOSE":
             fd, err = self._fd_from_stack(ins)
             if fd is not None and fd >= 0:
@@ -801,6 +893,55 @@ class Interpreter:
                 else:
                     stream.f.flush()
             self._push_io_status(err)
+
+    def _spawn(self, ins):
+        """SPAWN (io.c do_spawn): a command string and the child's stdin,
+        stdout and stderr descriptors (top of stack last); a null stream
+        (-1) gets a pipe whose other end becomes a new descriptor here.
+        The command is split at white space and run from PATH.  Leaves the
+        child's stderr, stdout and stdin descriptors, then the error string
+        and the success flag."""
+        import subprocess
+        st = self.stack
+        fds, err = [], None
+        for _ in range(3):  # err, out, in
+            fd, e = self._fd_from_stack(ins)
+            fds.append(fd)
+            err = err or e
+        err_fd, out_fd, in_fd = fds
+        cv = st.pop()
+        argv = "".join(map(chr, self.to_host(cv).tolist())).split()
+        self.drop(cv)
+        if err is None:
+            def target(fd, pipe):
+                return subprocess.PIPE if fd == NULL_STREAM_FD else self.files[fd].f.fileno()
+            free = [k for k in range(3, MAX_FILES) if k not in self.files]
+            if len(free) < [in_fd, out_fd, err_fd].count(NULL_STREAM_FD):
+                err = "no room in internal file table"
+            else:
+                for f in (self.files.get(k) for k in (in_fd, out_fd, err_fd)):
+                    if f is not None:
+                        f.f.flush()
+                try:
+                    proc = subprocess.Popen(argv, stdin=target(in_fd, 0), stdout=target(out_fd, 1),
+                                            stderr=target(err_fd, 2))
+                    new = []
+                    for fd, pipe in ((in_fd, proc.stdin), (out_fd, proc.stdout), (err_fd, proc.stderr)):
+                        if fd == NULL_STREAM_FD:
+                            k = free.pop(0)
+                            self.files[k] = _VStream(io.TextIOWrapper(pipe, encoding="latin-1", newline="",
+                                                                      write_through=True))
+                            new.append(k)
+                        else:
+                            new.append(fd)
+                    in_fd, out_fd, err_fd = new
+                except OSError as e:
+                    err = "SPAWN: error performing fork:" + (e.strerror or str(e))
+        if err is not None:
+            in_fd = out_fd = err_fd = NULL_STREAM_FD
+        for fd in (err_fd, out_fd, in_fd):
+            st.append(self.from_host("I", [fd]))
+        self._push_io_status(err)
 
     def _finish(self, nargs, results):
         st = self.stack

@@ -112,3 +112,126 @@ def test_fread_fwrite_program_on_gpu(gpu, oracle, tmp_path):
             it.free_all()
         assert fout.read_text() == "(" + "".join(f" {k}" for k in keys.tolist()) + " )\n"
     assert outs["gpu"] == outs["oracle"]
+
+
+_CHAR_RT = """FUNC RT
+COPY 1 1
+CONST INT 2
+FOPEN
+POP 2 0
+COPY 1 0
+CPOP 1 2
+CPOP 1 1
+FWRITE CHAR
+POP 2 0
+FCLOSE
+POP 2 0
+CONST INT 1
+FOPEN
+POP 2 0
+CONST CHAR ""
+CONST INT -1
+COPY 1 2
+FREAD_CHAR
+POP 2 0
+CPOP 1 2
+CONST CHAR "x"
+CONST INT 5
+COPY 1 2
+FREAD_CHAR
+POP 2 0
+CPOP 1 2
+CONST CHAR "x"
+CONST INT -1
+COPY 1 2
+FREAD_CHAR
+POP 2 0
+CPOP 1 2
+FCLOSE
+POP 2 0
+RET
+"""
+
+
+def test_fread_char_round_trip(oracle, tmp_path):
+    """FWRITE CHAR then FREAD_CHAR (io.c:1134-1300) give back every byte
+    value, \\r and \\n included (files are byte streams, no newline
+    translation); the stop status is -1 at the end of the file, -2 at the
+    character limit, else the delimiter, which is consumed."""
+    payload = list(range(1, 256)) + [13, 10, 13]
+    p = tmp_path / "chars.txt"
+    it = V.Interpreter(_CHAR_RT, oracle.cvl)
+    try:
+        st = it.run("RT", [it.from_host("I", _codes(str(p))), it.from_host("I", payload)])
+        got = [it.to_host(v).tolist() for v in st]
+    finally:
+        it.free_all()
+    assert p.read_bytes() == bytes(payload)
+    whole, stop1, five, stop2, rest, stop3 = got
+    assert whole == payload and stop1 == [-1]
+    assert five == [] and stop2 == [-1]  # the file is at its end: nothing left
+    assert rest == [] and stop3 == [-1]
+    q = tmp_path / "abc.txt"
+    q.write_bytes(b"abcdefxyz")
+    text = """FUNC RD
+CONST INT 1
+FOPEN
+POP 2 0
+CONST CHAR "x"
+CONST INT 4
+COPY 1 2
+FREAD_CHAR
+POP 2 0
+CPOP 1 2
+CONST CHAR "x"
+CONST INT -1
+COPY 1 2
+FREAD_CHAR
+POP 2 0
+CPOP 1 2
+POP 1 0
+RET
+"""
+    it = V.Interpreter(text, oracle.cvl)
+    try:
+        st = it.run("RD", [it.from_host("I", _codes(str(q)))])
+        got = [it.to_host(v).tolist() for v in st]
+    finally:
+        it.free_all()
+    assert got == [_codes("abcd"), [-2], _codes("ef"), [ord("x")]]
+
+
+def test_spawn_cat_round_trip(oracle):
+    """SPAWN (io.c do_spawn) of "cat -u" with pipes for its stdin and
+    stdout and the interpreter's stderr: a vector written to the child
+    comes back, as the reference suite's spawn test checks."""
+    text = """FUNC SP
+CONST CHAR "cat -u"
+CONST INT -1
+CONST INT -1
+CONST INT 2
+SPAWN
+POP 2 0
+CONST INT (23 -5 7)
+COPY 1 1
+FWRITE INT
+POP 2 0
+COPY 1 1
+FREAD INT
+POP 1 1
+CPOP 1 3
+FCLOSE
+POP 2 0
+CPOP 1 2
+FCLOSE
+POP 2 0
+POP 1 2
+RET
+"""
+    it = V.Interpreter(text, oracle.cvl)
+    try:
+        st = it.run("SP", [])
+        got = [it.to_host(v).tolist() for v in st]
+    finally:
+        it.free_all()
+    assert got == [[23, -5, 7], [1]]
