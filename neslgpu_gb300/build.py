@@ -78,12 +78,14 @@ def build_oracle(verbose: bool = False) -> Path:
     r = subprocess.run(["make", "-s", "-C", str(odir)], capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"oracle build failed:\n{r.stdout}\n{r.stderr}")
-    ref = Path(os.environ.get("GCVL_REFERENCE", "/root/reference")) / "nesl" / "cvl" / "serial"
-    if ref.is_dir():
-        r = subprocess.run(["make", "-s", "-C", str(odir), "ref",
-                            f"REF={ref.parent.parent}"], capture_output=True, text=True)
-        if r.returncode != 0 and verbose:
-            print("reference serial CVL not built:", r.stderr, file=sys.stderr)
+    # the oracle's Makefile knows where the reference tree is mounted
+    # (GCVL_REFERENCE overrides) and skips the build where it is not
+    args = ["make", "-s", "-C", str(odir), "ref"]
+    if os.environ.get("GCVL_REFERENCE"):
+        args.append(f"REF={Path(os.environ['GCVL_REFERENCE']) / 'nesl'}")
+    r = subprocess.run(args, capture_output=True, text=True)
+    if r.returncode != 0 and verbose:
+        print("reference serial CVL not built:", r.stderr, file=sys.stderr)
     return odir / "_build" / "libcvl_oracle.so"
 
 

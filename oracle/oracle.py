@@ -61,6 +61,21 @@ def load_reference():
     return _cache["ref"]
 
 
+def reference_root():
+    """The reference tree's root for tests that read its files: the
+    GCVL_REFERENCE environment variable, else the tree `make ref` built
+    oracle/_ref from; None where neither exists."""
+    import os
+    env = os.environ.get("GCVL_REFERENCE")
+    if env:
+        return Path(env) if Path(env).is_dir() else None
+    rec = ROOT / "_ref" / "REFERENCE"
+    if rec.exists():
+        p = Path(rec.read_text().strip())
+        return p if p.is_dir() else None
+    return None
+
+
 def now() -> float:
     return load_oracle().lib.ocvl_now()
 

@@ -14,14 +14,14 @@ recorded.  The program text itself is not stored.
     python tests/golden/make_nesltest_trace.py [reference root]
 
 writes tests/golden/nesltest_trace.npz.  The reference root defaults to
-$GCVL_REFERENCE, else /root/reference.
+the one oracle.oracle.reference_root() finds ($GCVL_REFERENCE, else the tree
+`make -C oracle ref` was built from).
 """
 from __future__ import annotations
 
 import contextlib
 import io
 import json
-import os
 import sys
 from pathlib import Path
 
@@ -133,7 +133,10 @@ def load(path=HERE / "nesltest_trace.npz"):
 
 
 def main():
-    ref = Path(sys.argv[1] if len(sys.argv) > 1 else os.environ.get("GCVL_REFERENCE", "/root/reference"))
+    from oracle.oracle import reference_root
+    ref = Path(sys.argv[1]) if len(sys.argv) > 1 else reference_root()
+    if ref is None:
+        sys.exit("no reference tree: pass its root, or set GCVL_REFERENCE")
     text = (ref / "nesl" / "vcode" / "nesltest.vcode").read_text(encoding="latin-1")
     records, report = record(text)
     np.savez_compressed(HERE / "nesltest_trace.npz", **pack(records, report))

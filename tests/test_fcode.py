@@ -12,7 +12,10 @@ from neslgpu_gb300 import fcode as F
 from neslgpu_gb300 import vcode as V
 from neslgpu_gb300 import vcode_programs as P
 
-REF_CU = sorted(glob.glob("/root/reference/bench/NESL/*.cu"))
+from oracle.oracle import reference_root
+
+_REF = reference_root()
+REF_CU = sorted(glob.glob(str(_REF / "bench" / "NESL" / "*.cu"))) if _REF else []
 
 
 def test_parse_and_emit_qsort_defs():

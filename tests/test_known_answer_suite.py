@@ -20,8 +20,6 @@ to nesl/vcode/nesltest.vcode and run by `make test` in nesl/vcode).
   stream: replay starts from the unseeded state, and every SRAND and RAND
   of the suite is replayed in order.
 """
-import os
-import re
 import sys
 from pathlib import Path
 
@@ -34,7 +32,10 @@ import make_nesltest_trace as T  # noqa: E402
 
 from neslgpu_gb300 import vcode as V  # noqa: E402
 
-REF_SUITE = Path(os.environ.get("GCVL_REFERENCE", "/root/reference")) / "nesl" / "vcode" / "nesltest.vcode"
+from oracle.oracle import reference_root  # noqa: E402
+
+_REF = reference_root()
+REF_SUITE = _REF / "nesl" / "vcode" / "nesltest.vcode" if _REF else Path("/nonexistent")
 EXPECTED_FAILED = ["checking the fail mechanism, failed message should appear", "rand (within range)"]
 SUMS = {"+_SCAN", "*_SCAN", "+_REDUCE", "*_REDUCE"}
 TRANSCENDENTAL = {"EXP", "LOG", "SIN", "COS", "TAN", "ASIN", "ACOS", "ATAN", "SINH", "COSH", "TANH"}

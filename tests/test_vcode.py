@@ -11,7 +11,10 @@ import pytest
 from neslgpu_gb300 import vcode as V
 from neslgpu_gb300 import vcode_programs as P
 
-REF_QS = "/root/reference/bench/NESL/qs.1000000.vcode"
+from oracle.oracle import reference_root
+
+_REF = reference_root()
+REF_QS = str(_REF / "bench" / "NESL" / "qs.1000000.vcode") if _REF else ""
 
 
 def _sort(cvl, keys, text=None, entry="QSORT"):

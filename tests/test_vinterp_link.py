@@ -16,7 +16,10 @@ from pathlib import Path
 import pytest
 
 ROOT = Path(__file__).resolve().parent.parent
-REF = Path(os.environ.get("GCVL_REFERENCE", "/root/reference")) / "nesl" / "vcode"
+from oracle.oracle import reference_root
+
+_REF = reference_root()
+REF = _REF / "nesl" / "vcode" if _REF else Path("/nonexistent")
 SOURCES = ["actions", "link_list", "main", "symbol_table", "program", "vcode_table", "rtstack", "stack",
            "vstack", "check_args", "cvl_table", "constant", "io", "vcode_hash", "fusion", "vcode-profile"]
 
