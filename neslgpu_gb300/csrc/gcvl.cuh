@@ -294,6 +294,12 @@ inline int lookback_units(int tiles) { return (int)((lookback_bytes(tiles) + 7) 
 bool scatter_partitioned_wanted(long n_d, size_t vsize);
 size_t scatter_partitioned_bytes(long n, size_t vsize);
 template <class V> void scatter_partitioned(V *d, const V *s, const int *idx, int n, int n_d, vec_p scratch);
+// Gathers d[k] = s[idx[k]] from a source larger than L2 absorbs random reads
+// from (rank.cu: partitioned by source window); scratch of
+// gather_partitioned_bytes.
+bool gather_partitioned_wanted(long n_src, long n, size_t vsize);
+size_t gather_partitioned_bytes(long n, size_t vsize);
+template <class V> void gather_partitioned(V *d, const V *s, const int *idx, int n, int n_src, vec_p scratch);
 
 __device__ __forceinline__ void lb_publish(ulonglong2 *w, unsigned long long status, unsigned long long bits) {
   asm volatile("{\n .reg .b128 t;\n mov.b128 t, {%1, %2};\n st.relaxed.gpu.global.b128 [%0], t;\n}"

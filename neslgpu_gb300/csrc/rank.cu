@@ -505,6 +505,123 @@ __global__ void __launch_bounds__(RK_BLOCK) k_window_scatter(V *__restrict__ d, 
   }
 }
 
+// ------------------------------------------------------- window split ---
+// Groups a tile's elements by the window of their key ((key >> shift) & 255,
+// 256 windows; the same bins as k_digit_hist's): slots within a window from
+// shared-memory atomics (in no particular order), the earlier tiles' count
+// of each window from the per-bin look-back, then every element written
+// straight to its slot from registers.  A window's slots of one tile are
+// consecutive and those of neighbouring tiles adjacent, so L2 merges the
+// writes into whole lines; nothing is staged or reordered in shared memory.
+// The partitioned gather uses it with POS (pos[k] = the slot element k went
+// to), the partitioned scatter with VAL (the value moves with its key).
+constexpr int WS_ITEMS = 16, WS_TILE = RK_BLOCK * WS_ITEMS;
+static_assert(WS_TILE == RK_TILE, "the window split shares the look-back state layout of the radix passes");
+template <class V, bool VAL, bool POS>
+__global__ void __launch_bounds__(RK_BLOCK) k_window_split(const unsigned *__restrict__ key,
+                                                           const V *__restrict__ val, long n, int shift,
+                                                           const unsigned *__restrict__ starts, unsigned *state,
+                                                           unsigned *counter, const unsigned *gate,
+                                                           unsigned *__restrict__ kout, V *__restrict__ vout,
+                                                           unsigned *__restrict__ pos, unsigned *status,
+                                                           int spin_limit) {
+  __shared__ unsigned s_cnt[256];
+  __shared__ unsigned s_base[256];
+  __shared__ unsigned s_tile;
+  if (gate && *(const volatile unsigned *)gate == 0) return;  // the same answer for every CTA
+  const int tid = threadIdx.x;
+  if (tid == 0) s_tile = atomicAdd(counter, 1u);  // tiles in dispatch order: predecessors are running
+  s_cnt[tid] = 0;
+  __syncthreads();
+  const int tile = (int)s_tile;
+  const long base = (long)tile * WS_TILE;
+  unsigned k[WS_ITEMS], r[WS_ITEMS];
+  V v[WS_ITEMS];
+#pragma unroll
+  for (int c = 0; c < WS_ITEMS; c++) {
+    const long e = base + c * RK_BLOCK + tid;
+    if (e < n) {
+      k[c] = __ldcs(key + e);
+      if (VAL) v[c] = __ldcs(val + e);
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < WS_ITEMS; c++)
+    if (base + c * RK_BLOCK + tid < n) r[c] = atomicAdd(&s_cnt[(k[c] >> shift) & 255u], 1u);
+  __syncthreads();
+  const unsigned prefix = bin_lookback(state, tile, tid, s_cnt[tid], status, spin_limit);
+  s_base[tid] = __ldg(starts + tid) + prefix;
+  __syncthreads();
+#pragma unroll
+  for (int c = 0; c < WS_ITEMS; c++) {
+    const long e = base + c * RK_BLOCK + tid;
+    if (e < n) {
+      const unsigned g = s_base[(k[c] >> shift) & 255u] + r[c];
+      kout[g] = k[c];
+      if (VAL) vout[g] = v[c];
+      if (POS) pos[e] = g;
+    }
+  }
+}
+
+// p[j] = s[key[j]] over keys that a window split grouped by source window:
+// CTAs dispatched in order keep the reads within a few windows of s, which
+// sit in L2 while they are read.  An index outside [0, n_src) reads nothing
+// (its value is 0) and sets DEV_RANGE.  p may be key itself (4-byte values).
+template <class V>
+__global__ void __launch_bounds__(RK_BLOCK) k_window_gather(V *p, const V *__restrict__ s, const unsigned *key,
+                                                            long n, unsigned n_src, const unsigned *gate,
+                                                            unsigned *status) {
+  if (gate && *(const volatile unsigned *)gate == 0) return;
+  const long i0 = (long)blockIdx.x * (RK_BLOCK * SC_ITEMS) + threadIdx.x;
+  unsigned k[SC_ITEMS];
+  V v[SC_ITEMS];
+#pragma unroll
+  for (int u = 0; u < SC_ITEMS; u++) {
+    const long i = i0 + (long)u * RK_BLOCK;
+    k[u] = i < n ? __ldcs(key + i) : 0u;
+  }
+  bool bad = false;
+#pragma unroll
+  for (int u = 0; u < SC_ITEMS; u++) {
+    v[u] = (V)0;
+    if (i0 + (long)u * RK_BLOCK < n) {
+      if (k[u] < n_src) v[u] = __ldg(s + k[u]);
+      else bad = true;
+    }
+  }
+  if (bad) atomicOr(status, DEV_RANGE);
+#pragma unroll
+  for (int u = 0; u < SC_ITEMS; u++) {
+    const long i = i0 + (long)u * RK_BLOCK;
+    if (i < n) p[i] = v[u];
+  }
+}
+
+// d[i] = s[idx[i]], run only when (*gate != 0) == when_set
+template <class V>
+__global__ void __launch_bounds__(RK_BLOCK) k_gather_gated(V *__restrict__ d, const V *__restrict__ s,
+                                                           const unsigned *__restrict__ idx, long n,
+                                                           const unsigned *gate, int when_set) {
+  if ((*(const volatile unsigned *)gate != 0) != (when_set != 0)) return;
+  const long i0 = (long)blockIdx.x * (RK_BLOCK * SC_ITEMS) + threadIdx.x;
+  unsigned k[SC_ITEMS];
+  V v[SC_ITEMS];
+#pragma unroll
+  for (int u = 0; u < SC_ITEMS; u++) {
+    const long i = i0 + (long)u * RK_BLOCK;
+    k[u] = i < n ? __ldcs(idx + i) : 0u;
+  }
+#pragma unroll
+  for (int u = 0; u < SC_ITEMS; u++)
+    if (i0 + (long)u * RK_BLOCK < n) v[u] = __ldg(s + k[u]);
+#pragma unroll
+  for (int u = 0; u < SC_ITEMS; u++) {
+    const long i = i0 + (long)u * RK_BLOCK;
+    if (i < n) __stcs(d + i, v[u]);
+  }
+}
+
 template <class K, class V, bool AUX, int IN, int OUT, bool STABLE = true>
 void launch_pass(const PassArgs<K, V> &a, int tiles) {
   constexpr size_t sm = pass_smem<K, V, AUX, STABLE>();
@@ -580,15 +697,86 @@ void scatter_partitioned(V *d, const V *s, const int *idx, int n, int n_d, vec_p
   const int g = sc_grid(n);
   k_sorted_scatter<V><<<g, RK_BLOCK, 0, S.stream>>>(d, s, idx, n, unsorted);
   launch_check("k_sorted_scatter");
-  PassArgs<unsigned, V> a{};
-  a.kin = (const unsigned *)idx; a.vin = s;
-  a.kout = (unsigned *)(mem + L.kout); a.vout = (V *)(mem + L.vout);
-  a.starts = hist; a.state = state; a.counter = counter; a.gate = unsorted;
-  a.n = n; a.shift = shift; a.status = S.d_status; a.spin_limit = S.spin_limit;
-  launch_pass<unsigned, V, false, IN_ARRAYS, OUT_ARRAYS, false>(a, tiles);
-  k_window_scatter<V><<<sc_blocks(n), RK_BLOCK, 0, S.stream>>>(d, a.kout, a.vout, n, unsorted);
+  unsigned *kout = (unsigned *)(mem + L.kout);
+  V *vout = (V *)(mem + L.vout);
+  k_window_split<V, true, false><<<tiles, RK_BLOCK, 0, S.stream>>>(
+      (const unsigned *)idx, s, n, shift, hist, state, counter, unsorted, kout, vout, nullptr, S.d_status,
+      S.spin_limit);
+  launch_check("k_window_split");
+  k_window_scatter<V><<<sc_blocks(n), RK_BLOCK, 0, S.stream>>>(d, kout, vout, n, unsorted);
   launch_check("k_window_scatter");
 }
+
+// ------------------------------------------------- partitioned gather ---
+// d[k] = s[idx[k]] for k < n (idx in [0, n_src)) when s is larger than L2 can
+// hold: random 4- or 8-byte reads from it each fetch a whole DRAM sector, and
+// most miss.  Instead: a histogram of the source windows of the indices
+// (which also tells whether they ascend), a window split of the indices
+// recording where each one went (pos), a gather in window order -- each
+// window of s read while it sits in L2 -- into p, and d[k] = p[pos[k]], whose
+// reads advance through 256 sequential runs of p at once.  All four passes
+// stream: 4 + 12 + 12 + 12 bytes per 4-byte element.  Ascending indices take
+// one plain gather instead (the device decides, as for the scatter).
+struct GatherLayout { size_t kout, pos, p, hist, counter, state, total; };
+inline GatherLayout gather_layout(long n, size_t vsize) {
+  GatherLayout L;
+  size_t o = 0;
+  auto take = [&](size_t bytes) { size_t at = o; o += align_up(bytes, 256); return at; };
+  L.kout = take((size_t)n * 4);
+  L.pos = take((size_t)n * 4);
+  L.p = vsize == 4 ? L.kout : take((size_t)n * vsize);  // 4-byte values overwrite their keys in place
+  L.hist = take(256 * 4);
+  L.counter = take(256);
+  L.state = take(rk_state_bytes(n));
+  L.total = o + 256;  // room to align the base
+  return L;
+}
+bool gather_partitioned_wanted(long n_src, long n, size_t vsize) {
+  return (size_t)n_src * vsize > ((size_t)64 << 20) && n >= (1L << 20);
+}
+size_t gather_partitioned_bytes(long n, size_t vsize) { return gather_layout(n, vsize).total; }
+
+template <class V>
+void gather_partitioned(V *d, const V *s, const int *idx, int n, int n_src, vec_p scratch) {
+  State &S = st();
+  if (n <= 0) return;
+  GatherLayout L = gather_layout(n, sizeof(V));
+  char *raw = (char *)scratch_or_work(scratch, L.total);
+  if (!raw) return;
+  char *mem = (char *)align_up((size_t)raw, 256);
+  unsigned *kout = (unsigned *)(mem + L.kout);
+  unsigned *pos = (unsigned *)(mem + L.pos);
+  V *p = (V *)(mem + L.p);
+  unsigned *hist = (unsigned *)(mem + L.hist);
+  unsigned *counter = (unsigned *)(mem + L.counter);
+  unsigned *state = (unsigned *)(mem + L.state);
+  unsigned *unsorted = counter + 1;  // the gate: non-zero when some index exceeds its successor
+  const int shift = window_shift(n_src);
+  const int tiles = rk_tiles(n);
+  GCVL_CK(cudaMemsetAsync(hist, 0, 256 * 4, S.stream));
+  GCVL_CK(cudaMemsetAsync(counter, 0, 8, S.stream));
+  GCVL_CK(cudaMemsetAsync(state, 0, rk_state_bytes(n), S.stream));
+  int hg = S.sm_count * 4;
+  if ((long)hg * RK_BLOCK > n) hg = (n + RK_BLOCK - 1) / RK_BLOCK;
+  k_digit_hist<<<hg, RK_BLOCK, 0, S.stream>>>((const unsigned *)idx, n, shift, hist, unsorted);
+  launch_check("k_digit_hist");
+  k_rank_digit_starts<<<1, 256, 0, S.stream>>>(hist, 1);
+  launch_check("k_rank_digit_starts");
+  k_gather_gated<V><<<sc_blocks(n), RK_BLOCK, 0, S.stream>>>(d, s, (const unsigned *)idx, n, unsorted, 0);
+  launch_check("k_gather_gated");
+  k_window_split<V, false, true><<<tiles, RK_BLOCK, 0, S.stream>>>(
+      (const unsigned *)idx, nullptr, n, shift, hist, state, counter, unsorted, kout, nullptr, pos, S.d_status,
+      S.spin_limit);
+  launch_check("k_window_split");
+  k_window_gather<V><<<sc_blocks(n), RK_BLOCK, 0, S.stream>>>(p, s, kout, n, (unsigned)n_src, unsorted,
+                                                              S.d_status);
+  launch_check("k_window_gather");
+  k_gather_gated<V><<<sc_blocks(n), RK_BLOCK, 0, S.stream>>>(d, p, pos, n, unsorted, 1);
+  launch_check("k_gather_gated");
+}
+template void gather_partitioned<unsigned>(unsigned *, const unsigned *, const int *, int, int, vec_p);
+template void gather_partitioned<unsigned long long>(unsigned long long *, const unsigned long long *,
+                                                     const int *, int, int, vec_p);
 template void scatter_partitioned<unsigned>(unsigned *, const unsigned *, const int *, int, int, vec_p);
 template void scatter_partitioned<unsigned long long>(unsigned long long *, const unsigned long long *,
                                                       const int *, int, int, vec_p);

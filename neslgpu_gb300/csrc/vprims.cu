@@ -246,6 +246,22 @@ template <class T> void gather(T *d, const T *s, const int *idx, long n, const c
 // bit moves: int and cvl_bool as 32-bit words, double as 64-bit words
 template <class T> struct Bits { typedef unsigned type; };
 template <> struct Bits<double> { typedef unsigned long long type; };
+// gather from a source of n_src elements: partitioned by source window when
+// the source is larger than L2 can serve random reads from
+template <class T> void gather_src(T *d, const T *s, const int *idx, int n, int n_src, vec_p scratch,
+                                   const char *name) {
+  typedef typename Bits<T>::type U;
+  if (n <= 0) return;
+  if (gather_partitioned_wanted(n_src, n, sizeof(T))) {
+    gather_partitioned<U>((U *)d, (const U *)s, idx, n, n_src, scratch);
+    return;
+  }
+  gather<T>(d, s, idx, n, name);
+}
+template <class T> int gather_units(int n_src, int n) {
+  if (n <= 0 || !gather_partitioned_wanted(n_src, n, sizeof(T))) return 0;
+  return (int)((gather_partitioned_bytes(n, sizeof(T)) + 7) / 8);
+}
 template <class T> void scatter(T *d, const T *s, const int *idx, int n, int n_d, vec_p scratch, const char *name) {
   typedef typename Bits<T>::type U;
   if (n <= 0) return;
@@ -646,14 +662,15 @@ META_SEG(ind_lez, INPLACE_NONE)
   GCVL_EXPORT unsigned smp_pe##L##_inplace(void) { return INPLACE_NONE; }               \
   GCVL_EXPORT void bck_pu##L(vec_p d, vec_p s, vec_p i, int s_len, int d_len,           \
                              vec_p scratch) {                                           \
-    (void)s_len; (void)scratch; ensure_init();                                          \
-    gather<T>((T *)d, (const T *)s, (const int *)i, d_len, "bck_pu" #L);                \
+    ensure_init();                                                                      \
+    gather_src<T>((T *)d, (const T *)s, (const int *)i, d_len, s_len, scratch, "bck_pu" #L); \
   }                                                                                     \
-  META2(bck_pu##L, INPLACE_2)                                                           \
+  GCVL_EXPORT int bck_pu##L##_scratch(int s_len, int d_len) { return gather_units<T>(s_len, d_len); } \
+  GCVL_EXPORT unsigned bck_pu##L##_inplace(void) { return INPLACE_2; }                  \
   GCVL_EXPORT void bck_pe##L(vec_p d, vec_p s, vec_p i, vec_p sd_s, int n_s, int m_s,   \
                              vec_p sd_d, int n_d, int m_d, vec_p scratch) {             \
-    (void)scratch; ensure_init();                                                       \
-    if (m_s == 1) { gather<T>((T *)d, (const T *)s, (const int *)i, n_d, "bck_pe" #L); return; } \
+    ensure_init();                                                                      \
+    if (m_s == 1) { gather_src<T>((T *)d, (const T *)s, (const int *)i, n_d, n_s, scratch, "bck_pe" #L); return; } \
     SegView ss = seg_view(sd_s, n_s, m_s);                                              \
     if (m_s == m_d)                                                                     \
       segmap(BPermMap<T>{(T *)d, (const T *)s, ss.off, (const int *)i},                  \
@@ -662,7 +679,10 @@ META_SEG(ind_lez, INPLACE_NONE)
       segwalk(BPermSeg<T>{(T *)d, (const T *)s, (const int *)i, ss.off, m_s},               \
               seg_view(sd_d, n_d, m_d), "bck_pe" #L);                                   \
   }                                                                                     \
-  META_SEG2(bck_pe##L, INPLACE_2)                                                       \
+  GCVL_EXPORT int bck_pe##L##_scratch(int n_s, int m_s, int n_d, int m_d) {              \
+    (void)m_d; return m_s == 1 ? gather_units<T>(n_s, n_d) : 0;                          \
+  }                                                                                     \
+  GCVL_EXPORT unsigned bck_pe##L##_inplace(void) { return INPLACE_2; }                  \
   GCVL_EXPORT void fpm_pu##L(vec_p d, vec_p s, vec_p i, vec_p f, int len_src,           \
                              int len_dest, vec_p scratch) {                             \
     (void)len_dest; (void)scratch; ensure_init();                                       \

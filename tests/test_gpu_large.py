@@ -155,3 +155,56 @@ def test_pack_two_pass_edges(gpu, oracle, n):
     x = r.integers(-2 ** 31, 2 ** 31, size=n, dtype=np.int64).astype(np.int32)
     for fl in (np.zeros(n, np.int32), np.ones(n, np.int32), (np.arange(n) % 2).astype(np.int32)):
         compare("exact", ops.pack_u(gpu, "pk2_luz", x, fl), ops.pack_u(oracle, "pk2_luz", x, fl))
+
+
+# The gather from a source larger than 64 MB takes the partitioned path
+# (indices split by source window, each window gathered while it sits in
+# L2, results put back in destination order); ascending indices take one
+# plain gather, decided on the device.
+NG = (1 << 24) + 77  # int32 source of 64 MB + 308 bytes
+
+
+@pytest.mark.parametrize("t,n_src,n_dst,kind", [
+    ("z", NG, NG, "perm"), ("d", (1 << 23) + 5, (1 << 23) + 5, "perm"), ("b", NG, NG, "dups"),
+    ("z", NG, NG, "ascending"), ("z", 1 << 25, (1 << 21) + 3, "dups"), ("d", 1 << 24, 3 << 22, "dups"),
+    ("z", NG, 1 << 20, "perm"), ("z", NG, NG, "window-edges"),
+])
+def test_gather_partitioned(gpu, oracle, t, n_src, n_dst, kind):
+    r = W.rng(n_src + n_dst)
+    if t == "d":
+        x = W.float64_normal(r, n_src)
+    elif t == "b":
+        x = r.integers(0, 2, size=n_src).astype(np.int32)
+    else:
+        x = r.integers(-(2 ** 31), 2 ** 31, size=n_src, dtype=np.int64).astype(np.int32)
+    if kind == "perm":
+        idx = r.permutation(n_src)[:n_dst].astype(np.int32)
+    elif kind == "ascending":
+        idx = np.sort(r.integers(0, n_src, size=n_dst)).astype(np.int32)
+    elif kind == "window-edges":  # the first and last element of every source window, and 0 and n-1
+        w = 1 << max(0, int(n_src - 1).bit_length() - 8)
+        edges = np.concatenate([np.arange(0, n_src, w), np.minimum(np.arange(w - 1, n_src + w, w), n_src - 1)])
+        idx = edges[r.integers(0, len(edges), size=n_dst)].astype(np.int32)
+    else:
+        idx = r.integers(0, n_src, size=n_dst).astype(np.int32)
+    got = ops.bck_u(gpu, f"bck_pu{t}", x, idx)
+    compare("exact", got, ops.bck_u(oracle, f"bck_pu{t}", x, idx))
+    # the same gather as a segmented one with one source segment
+    if n_src == n_dst:
+        one = np.array([n_src], dtype=np.int32)
+        compare("exact", ops.bck_e(gpu, f"bck_pe{t}", x, idx, one, one), got)
+
+
+def test_gather_partitioned_with_caller_scratch(gpu, oracle):
+    """As vinterp calls it: scratch sized by bck_puz_scratch, from the heap."""
+    c = gpu.cvl
+    r = W.rng(5)
+    x = r.integers(-(2 ** 31), 2 ** 31, size=NG, dtype=np.int64).astype(np.int32)
+    idx = r.permutation(NG).astype(np.int32)
+    units = c.bck_puz_scratch(NG, NG)
+    assert units > 0  # the partitioned path needs scratch
+    a, ix, d, scr = gpu.vec(x, "z"), gpu.vec(idx, "z"), gpu.out(NG, "z"), gpu.units(units)
+    c.bck_puz(d.ptr, a.ptr, ix.ptr, NG, NG, scr.ptr)
+    got = gpu.get(d, NG)
+    gpu.done()
+    compare("exact", got, ops.bck_u(oracle, "bck_puz", x, idx))
