@@ -303,6 +303,150 @@ template <class T> struct FPermSeg {  // if f[k]: d[off_d[seg_s(k)] + i[k]] = s[
       d[(long)__ldg(off_d + sg) + __ldg(i + k)] = __ldcs(s + k);
   }
 };
+// ------------------------------------------------ repeated destinations ---
+// The serial CVL's scatters with a default or flags (dpe_*, fpm_*, dfp_*;
+// nesl/cvl/serial/vecops.c) write element by element, so where elements
+// share a destination the last one's value stays.  NESL's library relies on
+// some value winning (remove_duplicates, union and intersection put with
+// repeated indices and read back which one won) and the reference's test
+// suite checks the serial answer.  Here the scatter itself lets any writer
+// win; a pass before it marks every destination in a bitmap (atomicOr; the
+// bitmap is n_d / 8 bytes, so it stays in L2) and raises a flag when one is
+// marked twice.  Only then do the gated passes after the scatter run: each
+// destination's largest source position (atomicMax), then a rewrite of the
+// destinations from their last writers.
+struct LwMem {
+  unsigned *bits, *flag;  // destination bitmap; flag word (+1: spare)
+  int *win;               // last writer per destination
+  int *gd;                // global destinations (segmented forms)
+  char *rest;             // what follows (the scatter's own scratch)
+};
+inline size_t lw_bytes(long n_s, long n_d, bool seg) {
+  return align_up((size_t)(n_d + 31) / 32 * 4 + 16, 256) + align_up((size_t)n_d * 4, 256) +
+         (seg ? align_up((size_t)n_s * 4, 256) : 0) + 256;
+}
+inline LwMem lw_carve(void *raw, long n_s, long n_d, bool seg) {
+  char *m = (char *)align_up((size_t)raw, 256);
+  LwMem L;
+  const size_t nb = (size_t)(n_d + 31) / 32 * 4;
+  L.bits = (unsigned *)m;
+  L.flag = (unsigned *)(m + nb);
+  m += align_up(nb + 16, 256);
+  L.win = (int *)m;
+  m += align_up((size_t)n_d * 4, 256);
+  L.gd = seg ? (int *)m : nullptr;
+  if (seg) m += align_up((size_t)n_s * 4, 256);
+  L.rest = m;
+  return L;
+}
+__device__ __forceinline__ bool lw_gate(const unsigned *flag) { return *(const volatile unsigned *)flag != 0; }
+__device__ __forceinline__ bool lw_mark(unsigned *bits, long g) {  // true if g was marked before
+  const unsigned b = 1u << (g & 31);
+  return (atomicOr(bits + (g >> 5), b) & b) != 0;
+}
+// destinations i[k] of the elements whose flag is set (all when f is null)
+__global__ void __launch_bounds__(VBLOCK) k_lw_detect(const int *__restrict__ i, const int *__restrict__ f, long n,
+                                                      long n_d, unsigned *bits, unsigned *flag) {
+  bool dup = false;
+  const long stride = (long)gridDim.x * VBLOCK;
+  for (long k = (long)blockIdx.x * VBLOCK + threadIdx.x; k < n; k += stride) {
+    if (f && !__ldg(f + k)) continue;
+    const long g = __ldg(i + k);
+    if (g >= 0 && g < n_d && lw_mark(bits, g)) dup = true;
+  }
+  if (dup) atomicOr(flag, 1u);
+}
+__global__ void __launch_bounds__(VBLOCK) k_lw_fill(int *win, long n_d, const unsigned *flag) {
+  if (!lw_gate(flag)) return;
+  const long stride = (long)gridDim.x * VBLOCK;
+  for (long j = (long)blockIdx.x * VBLOCK + threadIdx.x; j < n_d; j += stride) win[j] = -1;
+}
+__global__ void __launch_bounds__(VBLOCK) k_lw_max(const int *__restrict__ i, const int *__restrict__ f, long n,
+                                                   long n_d, int *win, const unsigned *flag) {
+  if (!lw_gate(flag)) return;
+  const long stride = (long)gridDim.x * VBLOCK;
+  for (long k = (long)blockIdx.x * VBLOCK + threadIdx.x; k < n; k += stride) {
+    if (f && !__ldg(f + k)) continue;
+    const long g = __ldg(i + k);
+    if (g >= 0 && g < n_d) atomicMax(win + g, (int)k);
+  }
+}
+template <class T>
+__global__ void __launch_bounds__(VBLOCK) k_lw_write(T *d, const T *__restrict__ s, const int *__restrict__ i,
+                                                     const int *__restrict__ f, long n, long n_d,
+                                                     const int *__restrict__ win, const unsigned *flag) {
+  if (!lw_gate(flag)) return;
+  const long stride = (long)gridDim.x * VBLOCK;
+  for (long k = (long)blockIdx.x * VBLOCK + threadIdx.x; k < n; k += stride) {
+    if (f && !__ldg(f + k)) continue;
+    const long g = __ldg(i + k);
+    if (g >= 0 && g < n_d && __ldg(win + g) == (int)k) d[g] = s[k];
+  }
+}
+// the segmented forms: the destination of k is off_d[segment of k] + i[k]
+struct LwDetectSeg {
+  const int *i; const int *f; const int *off_d; int m_d; long n_d; unsigned *bits; unsigned *flag;
+  __device__ void operator()(int k, int sg, int) const {
+    if (sg < m_d && (f == nullptr || __ldg(f + k))) {
+      const long g = (long)__ldg(off_d + sg) + __ldg(i + k);
+      if (g >= 0 && g < n_d && lw_mark(bits, g)) atomicOr(flag, 1u);
+    }
+  }
+};
+struct LwDestSeg {  // gd[k] = the global destination, or -1 (no write)
+  const int *i; const int *f; const int *off_d; int m_d; int *gd;
+  __device__ void operator()(int k, int sg, int) const {
+    gd[k] = (sg < m_d && (f == nullptr || __ldg(f + k))) ? __ldg(off_d + sg) + __ldg(i + k) : -1;
+  }
+};
+template <class F>
+__global__ void __launch_bounds__(VBLOCK) k_segwalk_gated(F f, SegView sv, const unsigned *flag) {
+  if (!lw_gate(flag)) return;
+  long k0 = ((long)blockIdx.x * VBLOCK + threadIdx.x) * SITEMS;
+  if (k0 >= sv.n) return;
+  int cnt = (int)min((long)SITEMS, (long)sv.n - k0);
+  int s = seg_of(sv, (int)k0);
+  int end = __ldg(sv.off + s + 1);
+  for (int q = 0; q < cnt; q++) {
+    int k = (int)k0 + q;
+    while (k >= end) { ++s; end = __ldg(sv.off + s + 1); }
+    f(k, s, 0);
+  }
+}
+inline int lw_grid(long n) {
+  long g = (n + VBLOCK - 1) / VBLOCK, cap = (long)st().sm_count * 16;
+  return (int)(g < 1 ? 1 : (g < cap ? g : cap));
+}
+// before the scatter: clear the bitmap and flag, mark the destinations
+inline void lw_detect(const LwMem &L, const int *i, const int *f, long n, long n_d) {
+  GCVL_CK(cudaMemsetAsync(L.bits, 0, (size_t)(n_d + 31) / 32 * 4 + 16, stream()));
+  if (n <= 0) return;
+  k_lw_detect<<<lw_grid(n), VBLOCK, 0, stream()>>>(i, f, n, n_d, L.bits, L.flag);
+  launch_check("k_lw_detect");
+}
+inline void lw_detect_seg(const LwMem &L, const int *i, const int *f, const SegView &ss, const SegView &sdd) {
+  GCVL_CK(cudaMemsetAsync(L.bits, 0, (size_t)(sdd.n + 31) / 32 * 4 + 16, stream()));
+  segwalk(LwDetectSeg{i, f, sdd.off, sdd.m, (long)sdd.n, L.bits, L.flag}, ss, "k_lw_detect_seg");
+}
+// after the scatter: the last writer of every destination, where some repeat
+template <class T> void lw_fix(T *d, const T *s, const LwMem &L, const int *i, const int *f, long n, long n_d) {
+  if (n <= 0 || n_d <= 0) return;
+  k_lw_fill<<<lw_grid(n_d), VBLOCK, 0, stream()>>>(L.win, n_d, L.flag);
+  launch_check("k_lw_fill");
+  k_lw_max<<<lw_grid(n), VBLOCK, 0, stream()>>>(i, f, n, n_d, L.win, L.flag);
+  launch_check("k_lw_max");
+  k_lw_write<T><<<lw_grid(n), VBLOCK, 0, stream()>>>(d, s, i, f, n, n_d, L.win, L.flag);
+  launch_check("k_lw_write");
+}
+template <class T> void lw_fix_seg(T *d, const T *s, const LwMem &L, const int *i, const int *f, const SegView &ss,
+                                   const SegView &sdd) {
+  if (ss.n <= 0 || ss.m <= 0) return;
+  k_segwalk_gated<<<grid_for(((long)ss.n + SITEMS - 1) / SITEMS, VBLOCK), VBLOCK, 0, stream()>>>(
+      LwDestSeg{i, f, sdd.off, sdd.m, L.gd}, ss, L.flag);
+  launch_check("k_lw_dest_seg");
+  lw_fix<T>(d, s, L, L.gd, nullptr, ss.n, sdd.n);
+}
+
 template <class T> struct BFPerm {  // d[k] = f[k] ? s[i[k]] : 0
   T *d; const T *s; const int *i; const int *f;
   __device__ void operator()(long k) const { d[k] = __ldg(f + k) ? __ldg(s + __ldg(i + k)) : (T)0; }
@@ -685,19 +829,36 @@ META_SEG(ind_lez, INPLACE_NONE)
   GCVL_EXPORT unsigned bck_pe##L##_inplace(void) { return INPLACE_2; }                  \
   GCVL_EXPORT void fpm_pu##L(vec_p d, vec_p s, vec_p i, vec_p f, int len_src,           \
                              int len_dest, vec_p scratch) {                             \
-    (void)len_dest; (void)scratch; ensure_init();                                       \
+    ensure_init();                                                                      \
+    if (len_src <= 0) return;                                                           \
+    void *mem = scratch_or_work(scratch, lw_bytes(len_src, len_dest, false));           \
+    if (!mem) return;                                                                   \
+    const LwMem W = lw_carve(mem, len_src, len_dest, false);                            \
+    lw_detect(W, (const int *)i, (const int *)f, len_src, len_dest);                    \
     each(FPerm<T>{(T *)d, (const T *)s, (const int *)i, (const int *)f}, len_src, "fpm_pu" #L); \
+    lw_fix<T>((T *)d, (const T *)s, W, (const int *)i, (const int *)f, len_src, len_dest); \
   }                                                                                     \
-  META2(fpm_pu##L, INPLACE_NONE)                                                        \
+  GCVL_EXPORT int fpm_pu##L##_scratch(int len_src, int len_dest) {                      \
+    return (int)((lw_bytes(len_src, len_dest, false) + 7) / 8);                         \
+  }                                                                                     \
+  GCVL_EXPORT unsigned fpm_pu##L##_inplace(void) { return INPLACE_NONE; }               \
   GCVL_EXPORT void fpm_pe##L(vec_p d, vec_p s, vec_p i, vec_p f, vec_p sd_s, int n_s,   \
                              int m_s, vec_p sd_d, int n_d, int m_d, vec_p scratch) {    \
-    (void)scratch; ensure_init();                                                       \
+    ensure_init();                                                                      \
     if (m_s == 1) { fpm_pu##L(d, s, i, f, n_s, n_d, scratch); return; }                 \
-    SegView sdd = seg_view(sd_d, n_d, m_d);                                             \
-    segwalk(FPermSeg<T>{(T *)d, (const T *)s, (const int *)i, (const int *)f, sdd.off, m_d}, \
-            seg_view(sd_s, n_s, m_s), "fpm_pe" #L);                                     \
+    if (n_s <= 0) return;                                                               \
+    void *mem = scratch_or_work(scratch, lw_bytes(n_s, n_d, true));                     \
+    if (!mem) return;                                                                   \
+    const LwMem W = lw_carve(mem, n_s, n_d, true);                                      \
+    SegView sdd = seg_view(sd_d, n_d, m_d), ss = seg_view(sd_s, n_s, m_s);              \
+    lw_detect_seg(W, (const int *)i, (const int *)f, ss, sdd);                          \
+    segwalk(FPermSeg<T>{(T *)d, (const T *)s, (const int *)i, (const int *)f, sdd.off, m_d}, ss, "fpm_pe" #L); \
+    lw_fix_seg<T>((T *)d, (const T *)s, W, (const int *)i, (const int *)f, ss, sdd);    \
   }                                                                                     \
-  META_SEG2(fpm_pe##L, INPLACE_NONE)                                                    \
+  GCVL_EXPORT int fpm_pe##L##_scratch(int n_s, int m_s, int n_d, int m_d) {             \
+    (void)m_d; return (int)((lw_bytes(n_s, n_d, m_s != 1) + 7) / 8);                    \
+  }                                                                                     \
+  GCVL_EXPORT unsigned fpm_pe##L##_inplace(void) { return INPLACE_NONE; }               \
   GCVL_EXPORT void bfp_pu##L(vec_p d, vec_p s, vec_p i, vec_p f, int len_src,           \
                              int len_dest, vec_p scratch) {                             \
     (void)len_src; (void)scratch; ensure_init();                                        \
@@ -717,10 +878,17 @@ META_SEG(ind_lez, INPLACE_NONE)
                              int len_dest, vec_p scratch) {                             \
     ensure_init();                                                                      \
     copy_dev<T>(d, v, len_dest);                                                        \
-    scatter<T>((T *)d, (const T *)s, (const int *)i, len_src, len_dest, scratch, "dpe_pu" #L); \
+    if (len_src <= 0) return;                                                           \
+    const size_t lb = lw_bytes(len_src, len_dest, false);                               \
+    char *mem = (char *)scratch_or_work(scratch, lb + (size_t)scatter_units<T>(len_src, len_dest) * 8); \
+    if (!mem) return;                                                                   \
+    const LwMem W = lw_carve(mem, len_src, len_dest, false);                            \
+    lw_detect(W, (const int *)i, nullptr, len_src, len_dest);                           \
+    scatter<T>((T *)d, (const T *)s, (const int *)i, len_src, len_dest, W.rest, "dpe_pu" #L); \
+    lw_fix<T>((T *)d, (const T *)s, W, (const int *)i, nullptr, len_src, len_dest);     \
   }                                                                                     \
   GCVL_EXPORT int dpe_pu##L##_scratch(int len_src, int len_dest) {                      \
-    return scatter_units<T>(len_src, len_dest);                                         \
+    return (int)((lw_bytes(len_src, len_dest, false) + 7) / 8) + scatter_units<T>(len_src, len_dest); \
   }                                                                                     \
   GCVL_EXPORT unsigned dpe_pu##L##_inplace(void) { return INPLACE_3; }                  \
   GCVL_EXPORT void dpe_pe##L(vec_p d, vec_p s, vec_p i, vec_p v, vec_p sd_s, int n_s,   \
@@ -728,12 +896,18 @@ META_SEG(ind_lez, INPLACE_NONE)
     ensure_init();                                                                      \
     if (m_s == 1) { dpe_pu##L(d, s, i, v, n_s, n_d, scratch); return; }                 \
     copy_dev<T>(d, v, n_d);                                                             \
-    SegView sdd = seg_view(sd_d, n_d, m_d);                                             \
-    segwalk(FPermSeg<T>{(T *)d, (const T *)s, (const int *)i, nullptr, sdd.off, m_d},   \
-            seg_view(sd_s, n_s, m_s), "dpe_pe" #L);                                     \
+    if (n_s <= 0) return;                                                               \
+    void *mem = scratch_or_work(scratch, lw_bytes(n_s, n_d, true));                     \
+    if (!mem) return;                                                                   \
+    const LwMem W = lw_carve(mem, n_s, n_d, true);                                      \
+    SegView sdd = seg_view(sd_d, n_d, m_d), ss = seg_view(sd_s, n_s, m_s);              \
+    lw_detect_seg(W, (const int *)i, nullptr, ss, sdd);                                 \
+    segwalk(FPermSeg<T>{(T *)d, (const T *)s, (const int *)i, nullptr, sdd.off, m_d}, ss, "dpe_pe" #L); \
+    lw_fix_seg<T>((T *)d, (const T *)s, W, (const int *)i, nullptr, ss, sdd);           \
   }                                                                                     \
   GCVL_EXPORT int dpe_pe##L##_scratch(int n_s, int m_s, int n_d, int m_d) {             \
-    (void)m_d; return m_s == 1 ? scatter_units<T>(n_s, n_d) : 0;                        \
+    (void)m_d;                                                                          \
+    return m_s == 1 ? dpe_pu##L##_scratch(n_s, n_d) : (int)((lw_bytes(n_s, n_d, true) + 7) / 8); \
   }                                                                                     \
   GCVL_EXPORT unsigned dpe_pe##L##_inplace(void) { return INPLACE_3; }                  \
   GCVL_EXPORT void dfp_pu##L(vec_p d, vec_p s, vec_p i, vec_p f, vec_p v, int len_src,  \
@@ -742,7 +916,8 @@ META_SEG(ind_lez, INPLACE_NONE)
     copy_dev<T>(d, v, len_dest);                                                        \
     fpm_pu##L(d, s, i, f, len_src, len_dest, scratch);                                  \
   }                                                                                     \
-  META2(dfp_pu##L, INPLACE_4)                                                           \
+  GCVL_EXPORT int dfp_pu##L##_scratch(int len_src, int len_dest) { return fpm_pu##L##_scratch(len_src, len_dest); } \
+  GCVL_EXPORT unsigned dfp_pu##L##_inplace(void) { return INPLACE_4; }                  \
   GCVL_EXPORT void dfp_pe##L(vec_p d, vec_p s, vec_p i, vec_p f, vec_p v, vec_p sd_s,   \
                              int n_s, int m_s, vec_p sd_d, int n_d, int m_d,            \
                              vec_p scratch) {                                           \
@@ -751,7 +926,10 @@ META_SEG(ind_lez, INPLACE_NONE)
     if (m_s == 1) fpm_pu##L(d, s, i, f, n_s, n_d, scratch);                             \
     else fpm_pe##L(d, s, i, f, sd_s, n_s, m_s, sd_d, n_d, m_d, scratch);                \
   }                                                                                     \
-  META_SEG2(dfp_pe##L, INPLACE_4)                                                       \
+  GCVL_EXPORT int dfp_pe##L##_scratch(int n_s, int m_s, int n_d, int m_d) {             \
+    return fpm_pe##L##_scratch(n_s, m_s, n_d, m_d);                                     \
+  }                                                                                     \
+  GCVL_EXPORT unsigned dfp_pe##L##_inplace(void) { return INPLACE_4; }                  \
   GCVL_EXPORT void pk2_lu##L(vec_p d, vec_p s, vec_p f, int src_len, int dest_len,      \
                              vec_p scratch) {                                           \
     (void)dest_len; pack<T>(d, s, f, src_len, scratch, "pk2_lu" #L);                    \

@@ -208,3 +208,33 @@ def test_gather_partitioned_with_caller_scratch(gpu, oracle):
     got = gpu.get(d, NG)
     gpu.done()
     compare("exact", got, ops.bck_u(oracle, "bck_puz", x, idx))
+
+
+# Scatters with a default or flags and repeated destinations: the serial CVL
+# writes element by element, so the last element aimed at a place wins
+# (nesl/cvl/serial/vecops.c); NESL's remove_duplicates, union and
+# intersection rely on that, and the reference's test suite checks it.
+@pytest.mark.parametrize("n,nd", [(1000, 700), (300_001, 100_003), ((1 << 23) + 4099, (1 << 23) + 4099)])
+@pytest.mark.parametrize("t", ["z", "d"])
+def test_default_permute_last_writer_wins(gpu, oracle, n, nd, t):
+    r = W.rng(n + nd)
+    x = W.float64_normal(r, n) if t == "d" else r.integers(-1000, 1000, size=n).astype(np.int32)
+    idx = r.integers(0, nd, size=n).astype(np.int32)  # many repeats
+    dflt = (np.full(nd, -7.5) if t == "d" else np.full(nd, -7, dtype=np.int32))
+    compare("exact", ops.dpe_u(gpu, f"dpe_pu{t}", x, idx, dflt), ops.dpe_u(oracle, f"dpe_pu{t}", x, idx, dflt))
+    flags = (r.random(n) < 0.6).astype(np.int32)
+    compare("exact", ops.fpm_u(gpu, f"fpm_pu{t}", x, idx, flags, nd), ops.fpm_u(oracle, f"fpm_pu{t}", x, idx, flags, nd))
+
+
+def test_segmented_default_permute_last_writer_wins(gpu, oracle):
+    r = W.rng(31)
+    lens = W.geometric_lengths(r, 400_000, 50.0)
+    n = int(lens.sum())
+    x = r.integers(-1000, 1000, size=n).astype(np.int32)
+    idx = (r.random(n) * np.repeat(lens, lens)).astype(np.int32)  # local indices, repeats within segments
+    dflt = np.full(n, -9, dtype=np.int32)
+    compare("exact", ops.dpe_e(gpu, "dpe_pez", x, idx, dflt, lens, lens),
+            ops.dpe_e(oracle, "dpe_pez", x, idx, dflt, lens, lens))
+    flags = (r.random(n) < 0.5).astype(np.int32)
+    compare("exact", ops.fpm_e(gpu, "fpm_pez", x, idx, flags, lens, lens),
+            ops.fpm_e(oracle, "fpm_pez", x, idx, flags, lens, lens))
