@@ -413,6 +413,89 @@ def _vcode_sort(cvl, keys, sync, fused=None):
         it.free_all()
 
 
+def graph_suite(c, sync, seed=7):
+    """VCODE basic blocks as CUDA graphs (vcode.Interpreter(graphs=True))
+    against plain launches, on programs that run again in the same state:
+    the same quicksort repeated (2^12 to 2^18 keys, where the interpreter's
+    and the launches' host time is a large part) and the SpMV program
+    repeated (2^14 and 2^22 rows).  Seconds per run: the median of the runs
+    after four warm-up runs (by then the heap has settled and every block
+    replays); results must equal the plain runs'."""
+    from neslgpu_gb300 import vcode as V, vcode_programs as P
+    r = np.random.default_rng(seed)
+    out = {}
+
+    def timed_runs(fn, reps):
+        ts, res = [], None
+        for _ in range(reps):
+            sync()
+            t0 = time.perf_counter()
+            res = fn()
+            sync()
+            ts.append(time.perf_counter() - t0)
+        return float(np.median(ts[4:])), res
+
+    for lg in (12, 16, 18):
+        keys = r.integers(-2 ** 31, 2 ** 31, size=1 << lg, dtype=np.int64).astype(np.int32)
+        row = {}
+        for mode in (False, True):
+            it = V.Interpreter(P.qsort_program(), c, sync=sync, graphs=mode)
+
+            def one():
+                lv = it.from_host("I", [len(keys)])
+                sd = it.segdes_from_lengths(lv)
+                it.drop(lv)
+                st = it.run("QSORT", [sd, it.from_host("I", keys)])
+                res = it.to_host(st[-1])
+                for v in st:
+                    it.drop(v)
+                return res
+            try:
+                t, res = timed_runs(one, 10)
+                row["graph" if mode else "plain"] = {"seconds": round(t, 6), "sorted": bool(np.array_equal(res, np.sort(keys)))}
+                if mode:
+                    row["graph"]["stats"] = dict(it.graph_stats)
+            finally:
+                it.free_all()
+        row["speedup"] = round(row["plain"]["seconds"] / row["graph"]["seconds"], 3)
+        out[f"quicksort_2e{lg}"] = row
+    for lg in (14, 22):
+        rows = 1 << lg
+        lens = np.minimum(r.zipf(2.1, size=rows), 1 << 16).astype(np.int32)
+        nnz = int(lens.sum(dtype=np.int64))
+        cols = r.integers(0, rows, size=nnz).astype(np.int32)
+        vals = r.standard_normal(nnz)
+        x = r.standard_normal(rows)
+        row, ys = {}, {}
+        for mode in (False, True):
+            it = V.Interpreter(P.spmv_program(), c, sync=sync, graphs=mode)
+            try:
+                lv = it.from_host("I", lens)
+                rsd = it.segdes_from_lengths(lv)
+                it.drop(lv)
+                args = [rsd, it.from_host("I", cols), it.from_host("F", vals), it.from_host("F", x)]
+
+                def one():
+                    for a in args:
+                        a.ref += 1  # the inputs stay across runs
+                    st = it.run("SPMV", list(args))
+                    y = it.to_host(st[0])
+                    it.drop(st[0])
+                    return y
+                t, ys[mode] = timed_runs(one, 12)
+                row["graph" if mode else "plain"] = {"seconds": round(t, 6)}
+                if mode:
+                    row["graph"]["stats"] = dict(it.graph_stats)
+                for a in args:
+                    it.drop(a)
+            finally:
+                it.free_all()
+        row["same_result"] = bool(np.array_equal(ys[False].view(np.int64), ys[True].view(np.int64)))
+        row["speedup"] = round(row["plain"]["seconds"] / row["graph"]["seconds"], 3)
+        out[f"spmv_2e{lg}_rows"] = row
+    return out
+
+
 def vinterp_suite(g, log2n=26, log2rows=22, seed=2026, cpu_sample_log2n=20):
     """The plain drop-in at scale through a VCODE interpreter: NESL
     quicksort (this repository's flattened VCODE program) on 2^log2n
@@ -513,7 +596,7 @@ def vinterp_suite(g, log2n=26, log2rows=22, seed=2026, cpu_sample_log2n=20):
                       "alg_gbs": round((nnz * (4 + 8 + 8) + 8 * rows + 4 * rows) / tf / 1e9, 1),
                       "speedup_vs_vcode": round(t / tf, 2),
                       "max_abs_diff_vs_vcode": float(np.max(np.abs(yf - yh)))}}
-    return {"quicksort": qs, "spmv": spmv}
+    return {"quicksort": qs, "spmv": spmv, "graph": graph_suite(c, sync)}
 
 
 def cpu_baseline_port(x, lens, threads=1):
@@ -882,6 +965,7 @@ def main():
     ap.add_argument("--batched-only", action="store_true", help="only the batched workload")
     ap.add_argument("--dispatch-only", action="store_true", help="only the learned-dispatcher sweep")
     ap.add_argument("--vinterp-only", action="store_true", help="only the VCODE programs")
+    ap.add_argument("--graph-only", action="store_true", help="only VCODE basic blocks as CUDA graphs")
     ap.add_argument("--dispatch-count", type=int, default=4096)
     ap.add_argument("--dispatch-hi", type=int, default=28)
     a = ap.parse_args()
@@ -894,6 +978,9 @@ def main():
         print(json.dumps({"primitives": primitive_suite(g, 1 << a.log2n, peaks()[0], only)}))
     elif a.batched_only:
         print(json.dumps({"batched": batched_suite(Gpu())}))
+    elif a.graph_only:
+        c = Gpu().c
+        print(json.dumps({"graph": graph_suite(c, lambda: c.gcvl_sync())}))
     elif a.vinterp_only:
         print(json.dumps({"vinterp": vinterp_suite(Gpu())}))
     elif a.dispatch_only:

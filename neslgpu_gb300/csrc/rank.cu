@@ -505,62 +505,176 @@ __global__ void __launch_bounds__(RK_BLOCK) k_window_scatter(V *__restrict__ d, 
   }
 }
 
-// ------------------------------------------------------- window split ---
-// Groups a tile's elements by the window of their key ((key >> shift) & 255,
-// 256 windows; the same bins as k_digit_hist's): slots within a window from
-// shared-memory atomics (in no particular order), the earlier tiles' count
-// of each window from the per-bin look-back, then every element written
-// straight to its slot from registers.  A window's slots of one tile are
-// consecutive and those of neighbouring tiles adjacent, so L2 merges the
-// writes into whole lines; nothing is staged or reordered in shared memory.
-// The partitioned gather uses it with POS (pos[k] = the slot element k went
-// to), the partitioned scatter with VAL (the value moves with its key).
-constexpr int WS_ITEMS = 16, WS_TILE = RK_BLOCK * WS_ITEMS;
-static_assert(WS_TILE == RK_TILE, "the window split shares the look-back state layout of the radix passes");
-template <class V, bool VAL, bool POS>
-__global__ void __launch_bounds__(RK_BLOCK) k_window_split(const unsigned *__restrict__ key,
-                                                           const V *__restrict__ val, long n, int shift,
-                                                           const unsigned *__restrict__ starts, unsigned *state,
-                                                           unsigned *counter, const unsigned *gate,
-                                                           unsigned *__restrict__ kout, V *__restrict__ vout,
-                                                           unsigned *__restrict__ pos, unsigned *status,
-                                                           int spin_limit) {
-  __shared__ unsigned s_cnt[256];
-  __shared__ unsigned s_base[256];
-  __shared__ unsigned s_tile;
-  if (gate && *(const volatile unsigned *)gate == 0) return;  // the same answer for every CTA
+// ------------------------------------------------------ window split ---
+// Groups keys by window (key >> shift, clamped below nw: the same function in
+// every pass) without any tile waiting on another: a histogram pass writes
+// each tile's per-window counts (window-major), a scan turns them into every
+// (window, tile)'s first slot, and the split pass places each tile's keys
+// there.  Slots within a window and tile come from shared-memory atomics (no
+// particular order); the tile is staged in shared memory by window and each
+// window's run leaves as one coalesced run; with POS, pos[k] = the slot key
+// k went to, written in the input order.  The partitioned gather uses it.
+constexpr int WS_ITEMS = 16, WS_TILE = RK_BLOCK * WS_ITEMS, WS_MAXW = 256;
+__device__ __forceinline__ unsigned ws_window(unsigned k, int shift, int nw) { return min(k >> shift, (unsigned)(nw - 1)); }
+
+// counts[w * tiles + t] = keys of tile t in window w; *unsorted != 0 when
+// some key exceeds its successor
+__global__ void __launch_bounds__(RK_BLOCK) k_ws_hist(const unsigned *__restrict__ key, long n, int shift, int nw,
+                                                      unsigned *__restrict__ counts, unsigned *unsorted) {
+  __shared__ unsigned s_cnt[WS_MAXW];
+  __shared__ int s_uns;
   const int tid = threadIdx.x;
-  if (tid == 0) s_tile = atomicAdd(counter, 1u);  // tiles in dispatch order: predecessors are running
+  const int tiles = gridDim.x, t = blockIdx.x;
   s_cnt[tid] = 0;
+  if (tid == 0) s_uns = 0;
   __syncthreads();
-  const int tile = (int)s_tile;
-  const long base = (long)tile * WS_TILE;
-  unsigned k[WS_ITEMS], r[WS_ITEMS];
-  V v[WS_ITEMS];
-#pragma unroll
+  const long base = (long)t * WS_TILE;
+  int uns = 0;
+#pragma unroll 4
   for (int c = 0; c < WS_ITEMS; c++) {
     const long e = base + c * RK_BLOCK + tid;
     if (e < n) {
-      k[c] = __ldcs(key + e);
-      if (VAL) v[c] = __ldcs(val + e);
+      const unsigned k = __ldcs(key + e);
+      atomicAdd(&s_cnt[ws_window(k, shift, nw)], 1u);
+      // the successor's load usually hits the line just read by the next lane
+      if (e + 1 < n && k > __ldg(key + e + 1)) uns = 1;
     }
+  }
+  if (__any_sync(0xffffffffu, uns) && (tid & 31) == 0) s_uns = 1;
+  __syncthreads();
+  if (tid < nw) counts[(long)tid * tiles + t] = s_cnt[tid];
+  if (tid == 0 && s_uns) atomicOr(unsorted, 1u);
+}
+
+// one CTA per window: totals[w] = its count over all tiles
+__global__ void __launch_bounds__(RK_BLOCK) k_ws_totals(const unsigned *__restrict__ counts, int tiles,
+                                                        unsigned *__restrict__ totals, const unsigned *gate) {
+  __shared__ unsigned s_ws[RK_WARPS];
+  if (!*(const volatile unsigned *)gate) return;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, w = blockIdx.x;
+  unsigned sum = 0;
+  for (int t = tid; t < tiles; t += RK_BLOCK) sum += __ldg(counts + (long)w * tiles + t);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
+  if (lane == 0) s_ws[warp] = sum;
+  __syncthreads();
+  if (tid == 0) {
+    unsigned tot = 0;
+#pragma unroll
+    for (int q = 0; q < RK_WARPS; q++) tot += s_ws[q];
+    totals[w] = tot;
+  }
+}
+
+// one CTA of WS_SCAN threads per window: counts[w][t] -> the first slot of
+// (w, t): the windows before w, then the tiles before t.  Each thread takes
+// WS_SCAN_ITEMS consecutive tiles at a time with all its loads in flight.
+constexpr int WS_SCAN = 1024, WS_SCAN_ITEMS = 8;
+__global__ void __launch_bounds__(WS_SCAN) k_ws_scan(unsigned *counts, int tiles, int nw,
+                                                     const unsigned *__restrict__ totals, const unsigned *gate) {
+  __shared__ unsigned s_ws[WS_SCAN / 32];
+  __shared__ unsigned s_start;
+  if (!*(const volatile unsigned *)gate) return;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, w = blockIdx.x;
+  if (tid == 0) {
+    unsigned st0 = 0;
+    for (int q = 0; q < w; q++) st0 += __ldg(totals + q);
+    s_start = st0;
+  }
+  unsigned *row = counts + (long)w * tiles;
+  __syncthreads();
+  unsigned carry = s_start;
+  for (int t0 = 0; t0 < tiles; t0 += WS_SCAN * WS_SCAN_ITEMS) {
+    const int tb = t0 + tid * WS_SCAN_ITEMS;
+    unsigned c[WS_SCAN_ITEMS];
+    unsigned sum = 0;
+#pragma unroll
+    for (int q = 0; q < WS_SCAN_ITEMS; q++) {
+      c[q] = tb + q < tiles ? row[tb + q] : 0u;
+      sum += c[q];
+    }
+    unsigned incl = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned x = shfl_up(incl, o);
+      if (lane >= o) incl += x;
+    }
+    if (lane == 31) s_ws[warp] = incl;
+    __syncthreads();
+    unsigned run = carry + incl - sum, all = 0;
+#pragma unroll 4
+    for (int q = 0; q < WS_SCAN / 32; q++) {
+      if (q < warp) run += s_ws[q];
+      all += s_ws[q];
+    }
+#pragma unroll
+    for (int q = 0; q < WS_SCAN_ITEMS; q++) {
+      if (tb + q < tiles) row[tb + q] = run;
+      run += c[q];
+    }
+    carry += all;
+    __syncthreads();  // s_ws is reused by the next chunk
+  }
+}
+
+template <bool POS>
+__global__ void __launch_bounds__(RK_BLOCK) k_window_split(const unsigned *__restrict__ key, long n, int shift,
+                                                           int nw, const unsigned *__restrict__ first,
+                                                           const unsigned *gate, unsigned *__restrict__ kout,
+                                                           unsigned *__restrict__ pos) {
+  __shared__ unsigned s_cnt[WS_MAXW];   // the tile's count per window, then its first slot there in the tile
+  __shared__ unsigned s_base[WS_MAXW];  // global slot of the window's first key of this tile
+  __shared__ unsigned s_key[WS_TILE];
+  __shared__ unsigned s_ws[RK_WARPS];
+  if (!*(const volatile unsigned *)gate) return;  // the same answer for every CTA
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int tiles = gridDim.x, t = blockIdx.x;
+  s_cnt[tid] = 0;
+  if (tid < nw) s_base[tid] = __ldg(first + (long)tid * tiles + t);
+  __syncthreads();
+  const long base = (long)t * WS_TILE;
+  const int valid = (int)min((long)WS_TILE, n - base);
+  unsigned k[WS_ITEMS], r[WS_ITEMS];
+#pragma unroll
+  for (int c = 0; c < WS_ITEMS; c++) {
+    const int e = c * RK_BLOCK + tid;
+    if (e < valid) k[c] = __ldcs(key + base + e);
   }
 #pragma unroll
   for (int c = 0; c < WS_ITEMS; c++)
-    if (base + c * RK_BLOCK + tid < n) r[c] = atomicAdd(&s_cnt[(k[c] >> shift) & 255u], 1u);
+    if (c * RK_BLOCK + tid < valid) r[c] = atomicAdd(&s_cnt[ws_window(k[c], shift, nw)], 1u);
   __syncthreads();
-  const unsigned prefix = bin_lookback(state, tile, tid, s_cnt[tid], status, spin_limit);
-  s_base[tid] = __ldg(starts + tid) + prefix;
+  // the windows' first slots within the tile: exclusive scan over the bins
+  const unsigned tot = s_cnt[tid];
+  unsigned incl = tot;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned x = shfl_up(incl, o);
+    if (lane >= o) incl += x;
+  }
+  if (lane == 31) s_ws[warp] = incl;
+  __syncthreads();
+  unsigned wp = 0;
+#pragma unroll
+  for (int q = 0; q < RK_WARPS; q++) if (q < warp) wp += s_ws[q];
+  s_cnt[tid] = wp + incl - tot;
   __syncthreads();
 #pragma unroll
   for (int c = 0; c < WS_ITEMS; c++) {
-    const long e = base + c * RK_BLOCK + tid;
-    if (e < n) {
-      const unsigned g = s_base[(k[c] >> shift) & 255u] + r[c];
-      kout[g] = k[c];
-      if (VAL) vout[g] = v[c];
-      if (POS) pos[e] = g;
+    const int e = c * RK_BLOCK + tid;
+    if (e < valid) {
+      const unsigned w = ws_window(k[c], shift, nw);
+      s_key[s_cnt[w] + r[c]] = k[c];
+      if (POS) pos[base + e] = s_base[w] + r[c];
     }
+  }
+  __syncthreads();
+  // coalesced runs: slot e of the tile holds window w's key e - s_cnt[w]
+#pragma unroll 4
+  for (int e = tid; e < valid; e += RK_BLOCK) {
+    const unsigned kk = s_key[e];
+    const unsigned w = ws_window(kk, shift, nw);
+    kout[s_base[w] + (unsigned)e - s_cnt[w]] = kk;
   }
 }
 
@@ -697,27 +811,28 @@ void scatter_partitioned(V *d, const V *s, const int *idx, int n, int n_d, vec_p
   const int g = sc_grid(n);
   k_sorted_scatter<V><<<g, RK_BLOCK, 0, S.stream>>>(d, s, idx, n, unsorted);
   launch_check("k_sorted_scatter");
-  unsigned *kout = (unsigned *)(mem + L.kout);
-  V *vout = (V *)(mem + L.vout);
-  k_window_split<V, true, false><<<tiles, RK_BLOCK, 0, S.stream>>>(
-      (const unsigned *)idx, s, n, shift, hist, state, counter, unsorted, kout, vout, nullptr, S.d_status,
-      S.spin_limit);
-  launch_check("k_window_split");
-  k_window_scatter<V><<<sc_blocks(n), RK_BLOCK, 0, S.stream>>>(d, kout, vout, n, unsorted);
+  PassArgs<unsigned, V> a{};
+  a.kin = (const unsigned *)idx; a.vin = s;
+  a.kout = (unsigned *)(mem + L.kout); a.vout = (V *)(mem + L.vout);
+  a.starts = hist; a.state = state; a.counter = counter; a.gate = unsorted;
+  a.n = n; a.shift = shift; a.status = S.d_status; a.spin_limit = S.spin_limit;
+  launch_pass<unsigned, V, false, IN_ARRAYS, OUT_ARRAYS, false>(a, tiles);
+  k_window_scatter<V><<<sc_blocks(n), RK_BLOCK, 0, S.stream>>>(d, a.kout, a.vout, n, unsorted);
   launch_check("k_window_scatter");
 }
 
 // ------------------------------------------------- partitioned gather ---
 // d[k] = s[idx[k]] for k < n (idx in [0, n_src)) when s is larger than L2 can
-// hold: random 4- or 8-byte reads from it each fetch a whole DRAM sector, and
-// most miss.  Instead: a histogram of the source windows of the indices
-// (which also tells whether they ascend), a window split of the indices
-// recording where each one went (pos), a gather in window order -- each
-// window of s read while it sits in L2 -- into p, and d[k] = p[pos[k]], whose
-// reads advance through 256 sequential runs of p at once.  All four passes
-// stream: 4 + 12 + 12 + 12 bytes per 4-byte element.  Ascending indices take
-// one plain gather instead (the device decides, as for the scatter).
-struct GatherLayout { size_t kout, pos, p, hist, counter, state, total; };
+// serve random reads from: each random 4- or 8-byte read from DRAM costs a
+// whole sector, and most miss.  Instead the indices are split by source
+// window (windows of about 32 MB, at most 256 of them), with pos[k] = where
+// index k went; a gather in window order reads each window of s while it
+// sits in L2, into p; and d[k] = p[pos[k]] reads p through as many sequential
+// runs as there are windows, few enough that L1 and L2 keep each run's
+// current lines.  The passes stream: 4 (histogram) + 12 (split) + 12 + 12
+// bytes per 4-byte element.  Ascending indices take one plain gather
+// instead; the device decides, as for the scatter.
+struct GatherLayout { size_t kout, pos, p, counts, totals, flags, total; };
 inline GatherLayout gather_layout(long n, size_t vsize) {
   GatherLayout L;
   size_t o = 0;
@@ -725,9 +840,9 @@ inline GatherLayout gather_layout(long n, size_t vsize) {
   L.kout = take((size_t)n * 4);
   L.pos = take((size_t)n * 4);
   L.p = vsize == 4 ? L.kout : take((size_t)n * vsize);  // 4-byte values overwrite their keys in place
-  L.hist = take(256 * 4);
-  L.counter = take(256);
-  L.state = take(rk_state_bytes(n));
+  L.counts = take((size_t)rk_tiles(n) * WS_MAXW * 4);
+  L.totals = take(WS_MAXW * 4);
+  L.flags = take(256);
   L.total = o + 256;  // room to align the base
   return L;
 }
@@ -747,26 +862,28 @@ void gather_partitioned(V *d, const V *s, const int *idx, int n, int n_src, vec_
   unsigned *kout = (unsigned *)(mem + L.kout);
   unsigned *pos = (unsigned *)(mem + L.pos);
   V *p = (V *)(mem + L.p);
-  unsigned *hist = (unsigned *)(mem + L.hist);
-  unsigned *counter = (unsigned *)(mem + L.counter);
-  unsigned *state = (unsigned *)(mem + L.state);
-  unsigned *unsorted = counter + 1;  // the gate: non-zero when some index exceeds its successor
-  const int shift = window_shift(n_src);
+  unsigned *counts = (unsigned *)(mem + L.counts);
+  unsigned *totals = (unsigned *)(mem + L.totals);
+  unsigned *unsorted = (unsigned *)(mem + L.flags);  // the gate: non-zero when some index exceeds its successor
+  // windows of about 32 MB of the source, a power of two from 2 to 256
+  const size_t src_bytes = (size_t)n_src * sizeof(V);
+  int wbits = 1;
+  while (wbits < 8 && (src_bytes >> wbits) > ((size_t)32 << 20)) ++wbits;
+  const int nb = bit_length((unsigned)(n_src > 1 ? n_src - 1 : 1));
+  const int shift = nb > wbits ? nb - wbits : 0;
+  const int nw = 1 << wbits;
   const int tiles = rk_tiles(n);
-  GCVL_CK(cudaMemsetAsync(hist, 0, 256 * 4, S.stream));
-  GCVL_CK(cudaMemsetAsync(counter, 0, 8, S.stream));
-  GCVL_CK(cudaMemsetAsync(state, 0, rk_state_bytes(n), S.stream));
-  int hg = S.sm_count * 4;
-  if ((long)hg * RK_BLOCK > n) hg = (n + RK_BLOCK - 1) / RK_BLOCK;
-  k_digit_hist<<<hg, RK_BLOCK, 0, S.stream>>>((const unsigned *)idx, n, shift, hist, unsorted);
-  launch_check("k_digit_hist");
-  k_rank_digit_starts<<<1, 256, 0, S.stream>>>(hist, 1);
-  launch_check("k_rank_digit_starts");
+  GCVL_CK(cudaMemsetAsync(unsorted, 0, 4, S.stream));
+  k_ws_hist<<<tiles, RK_BLOCK, 0, S.stream>>>((const unsigned *)idx, n, shift, nw, counts, unsorted);
+  launch_check("k_ws_hist");
   k_gather_gated<V><<<sc_blocks(n), RK_BLOCK, 0, S.stream>>>(d, s, (const unsigned *)idx, n, unsorted, 0);
   launch_check("k_gather_gated");
-  k_window_split<V, false, true><<<tiles, RK_BLOCK, 0, S.stream>>>(
-      (const unsigned *)idx, nullptr, n, shift, hist, state, counter, unsorted, kout, nullptr, pos, S.d_status,
-      S.spin_limit);
+  k_ws_totals<<<nw, RK_BLOCK, 0, S.stream>>>(counts, tiles, totals, unsorted);
+  launch_check("k_ws_totals");
+  k_ws_scan<<<nw, WS_SCAN, 0, S.stream>>>(counts, tiles, nw, totals, unsorted);
+  launch_check("k_ws_scan");
+  k_window_split<true><<<tiles, RK_BLOCK, 0, S.stream>>>((const unsigned *)idx, n, shift, nw, counts, unsorted,
+                                                         kout, pos);
   launch_check("k_window_split");
   k_window_gather<V><<<sc_blocks(n), RK_BLOCK, 0, S.stream>>>(p, s, kout, n, (unsigned)n_src, unsorted,
                                                               S.d_status);

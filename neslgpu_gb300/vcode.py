@@ -27,6 +27,7 @@ library or, for the parity tests and the CPU baseline, the oracle.
 """
 from __future__ import annotations
 
+import bisect
 import io
 import re
 import sys
@@ -79,6 +80,33 @@ class VcodeError(RuntimeError):
 
 # instructions a trace leaves out: host I/O and process control
 _UNTRACED = {"READ", "WRITE", "FREAD", "FWRITE", "FOPEN", "FCLOSE", "FREAD_CHAR", "SPAWN"}
+
+# Instructions that end a block captured as a CUDA graph: control flow, and
+# instructions that read a value back to the host (MAKE_SEGDES and PACK need
+# a length, IF a flag), write a host value into a new scalar (LENGTH), draw
+# from host-side state (RAND, SRAND), do I/O or time.
+_GRAPH_STOP = {"CALL", "RET", "IF", "ELSE", "ENDIF", "EXIT", "START_TIMER", "STOP_TIMER", "MAKE_SEGDES", "PACK",
+               "LENGTH", "RAND", "SRAND"} | _UNTRACED
+_HOST_ONLY = {"COPY", "POP", "CPOP", "CONST", "CONSTV"}
+
+
+class _NeedsHost(Exception):
+    """Raised inside a captured block when it would need the device
+    allocator (a new heap block, a larger scratch vector)."""
+
+
+class _NoLaunch:
+    """The CVL seen while a cached block's host bookkeeping is replayed:
+    size queries answer, every other call does nothing (the block's kernels
+    run as the cached graph instead)."""
+
+    def __init__(self, c):
+        self._c = c
+
+    def __getattr__(self, name):
+        if name.endswith("_scratch") or name.startswith("siz_"):
+            return getattr(self._c, name)
+        return lambda *a, **k: None
 
 
 # --------------------------------------------------------------- parse ---
@@ -217,6 +245,8 @@ class Heap:
         self.c = c
         self.free: dict[int, list[int]] = {}
         self.held = 0
+        self.no_new = False
+        self.on_trim = None  # called when blocks go back to the device
 
     @staticmethod
     def size_class(units: int) -> int:
@@ -228,6 +258,8 @@ class Heap:
         lst = self.free.get(cls)
         if lst:
             return lst.pop(), cls
+        if self.no_new:  # a captured or replayed block may not allocate
+            raise _NeedsHost("heap")
         p = self.c.alo_foz(cls)
         if not p:
             self.trim()
@@ -238,9 +270,16 @@ class Heap:
         return p, cls
 
     def release(self, ptr: int, cls: int):
-        self.free.setdefault(cls, []).append(ptr)
+        # each class's free list is kept in descending address order and
+        # allocation takes the lowest address: which addresses a sequence of
+        # requests gets then depends only on which blocks are free, not on
+        # the order they were freed in, so a block that runs again in the same
+        # state gets the same vectors (graph replay relies on it)
+        bisect.insort(self.free.setdefault(cls, []), ptr, key=lambda q: -q)
 
     def trim(self):
+        if self.on_trim:
+            self.on_trim()
         for cls, lst in self.free.items():
             for p in lst:
                 self.c.fre_fov(p)
@@ -352,12 +391,26 @@ class _VStream:
 class Interpreter:
     """Runs a parsed VCODE program on one CVL implementation."""
 
-    def __init__(self, text: str, cvl: CVL | None = None, sync=None, fused=None):
-        """fused: a FusedLib (neslgpu_gb300.fcode) for the program's FUSED ops."""
+    def __init__(self, text: str, cvl: CVL | None = None, sync=None, fused=None, graphs: bool = False,
+                 graph_min_ops: int = 2):
+        """fused: a FusedLib (neslgpu_gb300.fcode) for the program's FUSED ops.
+        graphs: run each basic block of at least graph_min_ops device
+        instructions as a CUDA graph, captured the first time the block runs
+        in a given state and replayed whenever it runs in that state again
+        (needs the library's gcvl_graph_* calls)."""
         self.fused = fused
+        self.graphs = graphs
+        self.graph_min_ops = graph_min_ops
+        self.graph_cache_max = 1024
+        self._block_ends: dict[int, int | None] = {}
+        self._graph_cache: dict = {}
+        self.graph_stats = {"captured": 0, "replayed": 0, "aborted": 0, "blocks_run": 0}
+        self._capturing = False
+        self._dry = False
         self.c = c = cvl or load()
         self.prog, self.funcs, self.main = parse(text)
         self.heap = Heap(c)
+        self.heap.on_trim = self.drop_graphs
         self.stack: list[Vec] = []
         self.scratch_ptr, self.scratch_units = 0, 0
         self._consts: dict = {}
@@ -408,6 +461,9 @@ class Interpreter:
 
     def scratch(self, units: int):
         if units > self.scratch_units:
+            if self._capturing or self._dry:
+                raise _NeedsHost("scratch")
+            self.drop_graphs()  # graphs hold the old scratch's address
             if self.scratch_ptr:
                 self.c.fre_fov(self.scratch_ptr)
             self.scratch_units = max(int(units), 2 * self.scratch_units, 1024)
@@ -416,7 +472,15 @@ class Interpreter:
                 raise MemoryError("scratch")
         return self.scratch_ptr
 
+    def drop_graphs(self):
+        """Forget the cached block graphs (the addresses they hold are about
+        to change)."""
+        for g in self._graph_cache.values():
+            self.c.gcvl_graph_destroy(g)
+        self._graph_cache.clear()
+
     def free_all(self):
+        self.drop_graphs()
         for v in self.stack:
             self.drop(v)
         self.stack.clear()
@@ -497,6 +561,12 @@ class Interpreter:
         rstack = [-1]
         t_start = None
         while pc >= 0:
+            if self.graphs:
+                end = self._block_end(pc)
+                if end is not None:
+                    self._run_block(pc, end)
+                    pc = end
+                    continue
             ins = prog[pc]
             op = ins.op
             pc += 1
@@ -554,6 +624,135 @@ class Interpreter:
             else:
                 self._vector_op(ins)
         return self.stack
+
+    # -- basic blocks as CUDA graphs
+    def _block_end(self, pc: int):
+        """End (exclusive) of the block of graph-capturable instructions that
+        starts at pc, or None when it holds too few device instructions."""
+        if pc in self._block_ends:
+            return self._block_ends[pc]
+        prog = self.prog
+        j, dev = pc, 0
+        while j < len(prog) and prog[j].op not in _GRAPH_STOP:
+            if prog[j].op not in _HOST_ONLY:
+                dev += 1
+            j += 1
+        end = j if dev >= self.graph_min_ops else None
+        self._block_ends[pc] = end
+        return end
+
+    def _exec_range(self, pc: int, end: int):
+        """Runs the straight-line instructions [pc, end) (no control flow)."""
+        st = self.stack
+        for ins in self.prog[pc:end]:
+            op = ins.op
+            self.ops_run += 1
+            if op == "COPY":
+                k, d = ins.a, ins.b
+                seg = st[len(st) - d - k: len(st) - d]
+                for v in seg:
+                    v.ref += 1
+                st.extend(seg)
+            elif op == "CPOP":
+                k, d = ins.a, ins.b
+                lo, hi = len(st) - d - k, len(st) - d
+                seg = st[lo:hi]
+                del st[lo:hi]
+                st.extend(seg)
+            elif op == "POP":
+                k, d = ins.a, ins.b
+                lo, hi = len(st) - d - k, len(st) - d
+                for v in st[lo:hi]:
+                    self.drop(v)
+                del st[lo:hi]
+            elif op == "CONST":
+                st.append(self._const(ins))
+            elif op == "CONSTV":
+                st.append(self._const_vec(ins))
+            else:
+                self._vector_op(ins)
+
+    def _block_key(self, pc: int):
+        """Everything the block's host bookkeeping depends on: the stack
+        (shapes, addresses, reference counts, which entries are one vector),
+        the heap's free lists in order, and the scratch vector."""
+        first: dict[int, int] = {}
+        ent = tuple((v.kind, v.len, v.seg_len, v.ptr, v.ref, v.const, first.setdefault(id(v), i))
+                    for i, v in enumerate(self.stack))
+        heap = tuple((c, tuple(lst)) for c, lst in sorted(self.heap.free.items()) if lst)
+        return pc, ent, heap, self.scratch_ptr, self.scratch_units
+
+    def _snapshot(self):
+        vecs = list(self.stack) + list(self._consts.values()) + list(self._scalar_cache.values())
+        return (list(self.stack), [(v, v.ref) for v in vecs], {c: list(lst) for c, lst in self.heap.free.items()},
+                self.heap.held)
+
+    def _restore(self, snap):
+        stack, refs, free, held = snap
+        self.stack[:] = stack
+        for v, r in refs:
+            v.ref = r
+        self.heap.free = free
+        self.heap.held = held
+
+    def _run_block(self, pc: int, end: int):
+        """Runs the block [pc, end) through a CUDA graph: replayed when the
+        block ran before in the same state (the host bookkeeping is redone
+        without calls, which yields the same vectors at the same addresses),
+        else captured while it runs and then launched; a capture that would
+        need the device allocator is abandoned, the state restored and the
+        block run plainly."""
+        c = self.c
+        self.graph_stats["blocks_run"] += 1
+        # constants first: their first use copies from the host
+        for ins in self.prog[pc:end]:
+            if ins.op == "CONST":
+                self.drop(self._const(ins))
+            elif ins.op == "CONSTV":
+                self.drop(self._const_vec(ins))
+        key = self._block_key(pc)
+        g = self._graph_cache.get(key)
+        if g is not None:
+            saved_c, saved_fn = self.c, self._fn
+            self.c, self._fn, self._dry, self.heap.no_new = _NoLaunch(saved_c), {}, True, True
+            try:
+                self._exec_range(pc, end)
+            finally:
+                self.c, self._fn, self._dry, self.heap.no_new = saved_c, saved_fn, False, False
+            if c.gcvl_graph_launch(g) != 0:
+                raise VcodeError(f"graph launch: {c.gcvl_error_string().decode()}")
+            self.graph_stats["replayed"] += 1
+            return
+        snap = self._snapshot()
+        if c.gcvl_graph_begin() != 0:
+            c.gcvl_clear_error()
+            self._exec_range(pc, end)
+            return
+        self._capturing, self.heap.no_new = True, True
+        try:
+            self._exec_range(pc, end)
+        except _NeedsHost:
+            self._capturing, self.heap.no_new = False, False
+            gx = c.gcvl_graph_end()
+            if gx:
+                c.gcvl_graph_destroy(gx)
+            c.gcvl_clear_error()
+            self._restore(snap)
+            self._exec_range(pc, end)
+            self.graph_stats["aborted"] += 1
+            return
+        finally:
+            self._capturing, self.heap.no_new = False, False
+        g = c.gcvl_graph_end()
+        if not g:
+            raise VcodeError(f"graph capture: {c.gcvl_error_string().decode()}")
+        if c.gcvl_graph_launch(g) != 0:
+            raise VcodeError(f"graph launch: {c.gcvl_error_string().decode()}")
+        self._graph_cache[key] = g
+        if len(self._graph_cache) > self.graph_cache_max:  # forget the oldest state
+            old = next(iter(self._graph_cache))
+            c.gcvl_graph_destroy(self._graph_cache.pop(old))
+        self.graph_stats["captured"] += 1
 
     def _traced_op(self, ins, depth: int = 8):
         """_vector_op, reporting the values it consumed and produced to
@@ -758,7 +957,8 @@ class Interpreter:
             a0 = args[0]
             L = a0.seg_len if a0.kind == "S" else a0.len
             d = self.new(fz.result_kind(k), L)
-            fz.fn[k](d.ptr, *[a.ptr for a in args], L, None)
+            if not self._dry:
+                fz.fn[k](d.ptr, *[a.ptr for a in args], L, None)
             self._finish(ar, [d])
         elif op == "SRAND":
             s = st[-1]
