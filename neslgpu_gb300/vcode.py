@@ -95,20 +95,6 @@ class _NeedsHost(Exception):
     allocator (a new heap block, a larger scratch vector)."""
 
 
-class _NoLaunch:
-    """The CVL seen while a cached block's host bookkeeping is replayed:
-    size queries answer, every other call does nothing (the block's kernels
-    run as the cached graph instead)."""
-
-    def __init__(self, c):
-        self._c = c
-
-    def __getattr__(self, name):
-        if name.endswith("_scratch") or name.startswith("siz_"):
-            return getattr(self._c, name)
-        return lambda *a, **k: None
-
-
 # --------------------------------------------------------------- parse ---
 @dataclass
 class Ins:
@@ -247,6 +233,7 @@ class Heap:
         self.held = 0
         self.no_new = False
         self.on_trim = None  # called when blocks go back to the device
+        self.log = None      # a list: every ("a"|"r", class, address) is appended
 
     @staticmethod
     def size_class(units: int) -> int:
@@ -257,7 +244,10 @@ class Heap:
         cls = self.size_class(units)
         lst = self.free.get(cls)
         if lst:
-            return lst.pop(), cls
+            p = lst.pop()
+            if self.log is not None:
+                self.log.append(("a", cls, p))
+            return p, cls
         if self.no_new:  # a captured or replayed block may not allocate
             raise _NeedsHost("heap")
         p = self.c.alo_foz(cls)
@@ -276,6 +266,8 @@ class Heap:
         # the order they were freed in, so a block that runs again in the same
         # state gets the same vectors (graph replay relies on it)
         bisect.insort(self.free.setdefault(cls, []), ptr, key=lambda q: -q)
+        if self.log is not None:
+            self.log.append(("r", cls, ptr))
 
     def trim(self):
         if self.on_trim:
@@ -403,10 +395,10 @@ class Interpreter:
         self.graph_min_ops = graph_min_ops
         self.graph_cache_max = 1024
         self._block_ends: dict[int, int | None] = {}
-        self._graph_cache: dict = {}
+        self._blocks: dict[int, dict] = {}  # pc -> {"recs": {depth: {signature: [record]}}, "warm": bool}
+        self._n_graphs = 0
         self.graph_stats = {"captured": 0, "replayed": 0, "aborted": 0, "blocks_run": 0}
         self._capturing = False
-        self._dry = False
         self.c = c = cvl or load()
         self.prog, self.funcs, self.main = parse(text)
         self.heap = Heap(c)
@@ -461,7 +453,7 @@ class Interpreter:
 
     def scratch(self, units: int):
         if units > self.scratch_units:
-            if self._capturing or self._dry:
+            if self._capturing:
                 raise _NeedsHost("scratch")
             self.drop_graphs()  # graphs hold the old scratch's address
             if self.scratch_ptr:
@@ -475,9 +467,13 @@ class Interpreter:
     def drop_graphs(self):
         """Forget the cached block graphs (the addresses they hold are about
         to change)."""
-        for g in self._graph_cache.values():
-            self.c.gcvl_graph_destroy(g)
-        self._graph_cache.clear()
+        for info in self._blocks.values():
+            for by_sig in info["recs"].values():
+                for recs in by_sig.values():
+                    for r in recs:
+                        self.c.gcvl_graph_destroy(r["graph"])
+            info["recs"].clear()
+        self._n_graphs = 0
 
     def free_all(self):
         self.drop_graphs()
@@ -672,15 +668,14 @@ class Interpreter:
             else:
                 self._vector_op(ins)
 
-    def _block_key(self, pc: int):
-        """Everything the block's host bookkeeping depends on: the stack
-        (shapes, addresses, reference counts, which entries are one vector),
-        the heap's free lists in order, and the scratch vector."""
+    @staticmethod
+    def _stack_sig(top, refs=None) -> tuple:
+        """Shapes, addresses, reference counts (refs: id -> count, else the
+        current ones) and aliasing of stack entries.  A cached constant's
+        count is left out: it is never freed, so the count changes nothing."""
         first: dict[int, int] = {}
-        ent = tuple((v.kind, v.len, v.seg_len, v.ptr, v.ref, v.const, first.setdefault(id(v), i))
-                    for i, v in enumerate(self.stack))
-        heap = tuple((c, tuple(lst)) for c, lst in sorted(self.heap.free.items()) if lst)
-        return pc, ent, heap, self.scratch_ptr, self.scratch_units
+        return tuple((v.kind, v.len, v.seg_len, v.ptr, -1 if v.const else (v.ref if refs is None else refs[id(v)]),
+                      v.const, first.setdefault(id(v), i)) for i, v in enumerate(top))
 
     def _snapshot(self):
         vecs = list(self.stack) + list(self._consts.values()) + list(self._scalar_cache.values())
@@ -695,44 +690,83 @@ class Interpreter:
         self.heap.free = free
         self.heap.held = held
 
-    def _run_block(self, pc: int, end: int):
-        """Runs the block [pc, end) through a CUDA graph: replayed when the
-        block ran before in the same state (the host bookkeeping is redone
-        without calls, which yields the same vectors at the same addresses),
-        else captured while it runs and then launched; a capture that would
-        need the device allocator is abandoned, the state restored and the
-        block run plainly."""
-        c = self.c
-        self.graph_stats["blocks_run"] += 1
-        # constants first: their first use copies from the host
-        for ins in self.prog[pc:end]:
-            if ins.op == "CONST":
-                self.drop(self._const(ins))
-            elif ins.op == "CONSTV":
-                self.drop(self._const_vec(ins))
-        key = self._block_key(pc)
-        g = self._graph_cache.get(key)
-        if g is not None:
-            saved_c, saved_fn = self.c, self._fn
-            self.c, self._fn, self._dry, self.heap.no_new = _NoLaunch(saved_c), {}, True, True
-            try:
-                self._exec_range(pc, end)
-            finally:
-                self.c, self._fn, self._dry, self.heap.no_new = saved_c, saved_fn, False, False
-            if c.gcvl_graph_launch(g) != 0:
-                raise VcodeError(f"graph launch: {c.gcvl_error_string().decode()}")
-            self.graph_stats["replayed"] += 1
-            return
+    def _replay(self, info, pc: int, end: int) -> bool:
+        """Runs the block from its graph if one was captured in the state the
+        block now reads: the top `depth` stack entries, the lowest free
+        addresses of each size class it allocates from (allocation takes the
+        lowest) and the scratch vector.  The host side is the recorded
+        effect: stack rewrite, reference counts, heap operations."""
+        st = self.stack
+        free = self.heap.free
+        rec = None
+        for D, by_sig in info["recs"].items():  # the depths the block reached in the states it was captured in
+            if len(st) < D:
+                continue
+            base = len(st) - D
+            top = st[base:]
+            for r in by_sig.get(self._stack_sig(top), ()):
+                if r["scratch"] != (self.scratch_ptr, self.scratch_units):
+                    continue
+                if all(len(free.get(c, ())) >= len(req) and tuple(free[c][len(free[c]) - len(req):]) == req
+                       for c, req in r["req"].items()):
+                    rec = r
+                    break
+            if rec is not None:
+                break
+        if rec is None:
+            return False
+        news = []
+        for kind, ln, sl, ptr, cls, ref in rec["new"]:
+            v = Vec(kind, ln, sl, ptr, cls)
+            v.ref = ref
+            news.append(v)
+        for i, delta in rec["refs"]:
+            top[i].ref += delta
+        for op, c, ptr in rec["log"]:
+            if op == "a":
+                free[c].pop()
+            else:
+                bisect.insort(free.setdefault(c, []), ptr, key=lambda q: -q)
+        st[base:] = [top[j] if w == "o" else (news[j] if w == "n" else j) for w, j in rec["out"]]
+        self.ops_run += end - pc
+        if self.c.gcvl_graph_launch(rec["graph"]) != 0:
+            raise VcodeError(f"graph launch: {self.c.gcvl_error_string().decode()}")
+        self.graph_stats["replayed"] += 1
+        return True
+
+    def _capture(self, info, pc: int, end: int):
+        """Runs the block while capturing its calls into a graph, then
+        launches the graph and records the block's host effect for replay.
+        Abandoned (state restored, block run plainly) when the block would
+        need the device allocator."""
+        c, st = self.c, self.stack
         snap = self._snapshot()
         if c.gcvl_graph_begin() != 0:
             c.gcvl_clear_error()
             self._exec_range(pc, end)
             return
-        self._capturing, self.heap.no_new = True, True
+        start = list(st)
+        L0 = len(start)
+        start_ref = {id(v): v.ref for v in start}
+        lowest = L0
+        self._capturing, self.heap.no_new, self.heap.log = True, True, []
         try:
-            self._exec_range(pc, end)
+            for q in range(pc, end):  # _exec_range, noting the lowest stack entry each instruction reaches
+                ins = self.prog[q]
+                if ins.op in ("COPY", "POP", "CPOP"):
+                    lowest = min(lowest, len(st) - ins.b - ins.a)
+                    self._exec_range(q, q + 1)
+                elif ins.op in ("CONST", "CONSTV"):
+                    self._exec_range(q, q + 1)
+                else:
+                    before = list(st)
+                    self._exec_range(q, q + 1)
+                    p = 0
+                    while p < len(before) and p < len(st) and st[p] is before[p]:
+                        p += 1
+                    lowest = min(lowest, p)
         except _NeedsHost:
-            self._capturing, self.heap.no_new = False, False
+            self._capturing, self.heap.no_new, self.heap.log = False, False, None
             gx = c.gcvl_graph_end()
             if gx:
                 c.gcvl_graph_destroy(gx)
@@ -742,17 +776,64 @@ class Interpreter:
             self.graph_stats["aborted"] += 1
             return
         finally:
-            self._capturing, self.heap.no_new = False, False
+            log = self.heap.log
+            self._capturing, self.heap.no_new, self.heap.log = False, False, None
         g = c.gcvl_graph_end()
         if not g:
             raise VcodeError(f"graph capture: {c.gcvl_error_string().decode()}")
         if c.gcvl_graph_launch(g) != 0:
             raise VcodeError(f"graph launch: {c.gcvl_error_string().decode()}")
-        self._graph_cache[key] = g
-        if len(self._graph_cache) > self.graph_cache_max:  # forget the oldest state
-            old = next(iter(self._graph_cache))
-            c.gcvl_graph_destroy(self._graph_cache.pop(old))
         self.graph_stats["captured"] += 1
+        if self._n_graphs >= self.graph_cache_max:
+            c.gcvl_graph_destroy(g)
+            return
+        D = L0 - lowest
+        top = start[lowest:]
+        pos = {}
+        for i, v in enumerate(top):
+            pos.setdefault(id(v), i)
+        new_ix: dict[int, int] = {}
+        new_spec, out = [], []
+        for v in st[lowest:]:
+            if id(v) in pos:
+                out.append(("o", pos[id(v)]))
+            elif v.const:
+                out.append(("c", v))  # a cached constant: the same vector
+            else:
+                if id(v) not in new_ix:
+                    new_ix[id(v)] = len(new_spec)
+                    new_spec.append((v.kind, v.len, v.seg_len, v.ptr, v.cls, v.ref))
+                out.append(("n", new_ix[id(v)]))
+        refs = [(i, top[i].ref - start_ref[id(top[i])]) for i in sorted(set(pos.values()))
+                if top[i].ref != start_ref[id(top[i])]]
+        initial_free = snap[2]
+        allocs: dict[int, int] = {}
+        for op, cls, _ in log:
+            if op == "a":
+                allocs[cls] = allocs.get(cls, 0) + 1
+        req = {cls: tuple(initial_free[cls][len(initial_free[cls]) - k:]) for cls, k in allocs.items()}
+        rec = {"graph": g, "req": req, "scratch": (self.scratch_ptr, self.scratch_units), "new": new_spec,
+               "refs": refs, "log": log, "out": out}
+        info["recs"].setdefault(D, {}).setdefault(self._stack_sig(top, start_ref), []).append(rec)
+        self._n_graphs += 1
+
+    def _run_block(self, pc: int, end: int):
+        """Runs the block [pc, end) through a CUDA graph: replayed when it ran
+        before in the state it reads now, else captured while it runs."""
+        self.graph_stats["blocks_run"] += 1
+        info = self._blocks.get(pc)
+        if info is None:
+            info = self._blocks[pc] = {"recs": {}, "warm": False}
+        if not info["warm"]:
+            # constants first: their first use copies from the host
+            for ins in self.prog[pc:end]:
+                if ins.op == "CONST":
+                    self.drop(self._const(ins))
+                elif ins.op == "CONSTV":
+                    self.drop(self._const_vec(ins))
+            info["warm"] = True
+        if not self._replay(info, pc, end):
+            self._capture(info, pc, end)
 
     def _traced_op(self, ins, depth: int = 8):
         """_vector_op, reporting the values it consumed and produced to
@@ -957,8 +1038,7 @@ class Interpreter:
             a0 = args[0]
             L = a0.seg_len if a0.kind == "S" else a0.len
             d = self.new(fz.result_kind(k), L)
-            if not self._dry:
-                fz.fn[k](d.ptr, *[a.ptr for a in args], L, None)
+            fz.fn[k](d.ptr, *[a.ptr for a in args], L, None)
             self._finish(ar, [d])
         elif op == "SRAND":
             s = st[-1]

@@ -126,6 +126,12 @@ def test_quicksort_blocks_on_oracle(oracle, n):
         assert np.array_equal(got, np.sort(keys))
     if n >= 3000:
         assert it.graph_stats["replayed"] > 0, it.graph_stats
+        # settled: a further run replays every block and captures none
+        before = dict(it.graph_stats)
+        got, it = _sort(fake, keys, True, it)
+        assert np.array_equal(got, np.sort(keys))
+        assert it.graph_stats["captured"] == before["captured"], (before, it.graph_stats)
+        assert it.graph_stats["replayed"] - before["replayed"] == it.graph_stats["blocks_run"] - before["blocks_run"]
     it.free_all()
 
 
