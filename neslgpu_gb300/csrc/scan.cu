@@ -662,6 +662,22 @@ __global__ void __launch_bounds__(cta_threads<MODE>(), MODE == M_REDUCE ? (sizeo
       if (!pf) a.lead[tile] = first_s;  // began in an earlier tile
     }
   } else {  // M_REDUCE: results at segment ends
+    // float64 +: pieces between heads, each summed in fixed point.  Element
+    // i ends a non-empty segment exactly when element i+1 is a head (or past
+    // the end): only those positions are visited (mostly none).  Whether the
+    // warp chains its items is decided by every lane, those past the
+    // vector's end too (they hold no ends): a warp vote must not name lanes
+    // that are elsewhere.
+    unsigned ends = 0;
+    bool chain_warp = false;
+    if constexpr (std::is_same<Op, AddD>::value) {
+      if (cnt > 0) {
+        const int kn = k0 + cnt;
+        const unsigned nh = kn >= a.n ? 1u : (__ldg(a.sv.bits + (kn >> 5)) >> (kn & 31)) & 1u;
+        ends = ((heads >> 1) | (nh << (cnt - 1))) & (cnt >= 32 ? ~0u : ((1u << cnt) - 1u));
+      }
+      if (CHAIN) chain_warp = __any_sync(0xffffffffu, __popc(ends) >= 2);
+    }
     if (cnt > 0) {
       const int m = a.sv.m;
       if (k0 == 0)
@@ -669,13 +685,7 @@ __global__ void __launch_bounds__(cta_threads<MODE>(), MODE == M_REDUCE ? (sizeo
       int s = s0;
       int end = off(s + 1);
       if constexpr (std::is_same<Op, AddD>::value) {
-        // pieces between heads, each summed in fixed point.  Element i ends
-        // a non-empty segment exactly when element i+1 is a head (or past
-        // the end): only those positions are visited (mostly none).
-        const int kn = k0 + cnt;
-        const unsigned nh = kn >= a.n ? 1u : (__ldg(a.sv.bits + (kn >> 5)) >> (kn & 31)) & 1u;
-        unsigned ends = ((heads >> 1) | (nh << (cnt - 1))) & (cnt >= 32 ? ~0u : ((1u << cnt) - 1u));
-        if (CHAIN && __any_sync(0xffffffffu, __popc(ends) >= 2)) {
+        if (chain_warp) {
           // short segments: one FP64 add per item beats a fixed-point pass
           // per segment end (each a separate sum of up to 16 items)
           double r = run;
