@@ -889,7 +889,13 @@ __device__ __forceinline__ void ring_arm(int t, unsigned long long *bar, unsigne
 // already gave up (a timeout is flagged); otherwise the load is long done.
 constexpr int kRingDrain = kDrainLimit;
 
-template <class Op, bool SEG>
+// RED: a segmented reduction instead of a scan (not float64 +, whose
+// fixed-point fold would bind the ALU without the scan's output chain to
+// hide behind): the same fold, publication and look-back, and in the second
+// round each thread that ends segments writes their results (a.out has one
+// per segment) from the exclusive prefix and a fold of its piece; nothing is
+// stored back, so the slot is freed as soon as its rows are read.
+template <class Op, bool SEG, bool RED = false>
 __global__ void __launch_bounds__(RTB, GCVL_RING_MINB)
     k_scan_ring(const __grid_constant__ CUtensorMap tin, const __grid_constant__ CUtensorMap tout,
                 TArgs<typename Op::T> a, int tiles) {
@@ -1040,6 +1046,36 @@ __global__ void __launch_bounds__(RTB, GCVL_RING_MINB)
         T x[ITEMS];
         unsigned char *buf = ring + ps * TILE_BYTES;
         row_load<Op, ITEMS>(x, buf, tid, in_map, a.in, k0, cnt);
+        if constexpr (RED) {
+          named_arrive(3, RTB);  // the rows are read: the look-back warp may reuse the slot
+          // element i ends a non-empty segment exactly when element i+1 is a
+          // head (or past the end)
+          unsigned ends = 0;
+          if (cnt > 0) {
+            const int kn = k0 + cnt;
+            const unsigned nh = kn >= a.n ? 1u : (__ldg(a.sv.bits + (kn >> 5)) >> (kn & 31)) & 1u;
+            ends = ((p_heads >> 1) | (nh << (cnt - 1))) & (cnt >= 32 ? ~0u : ((1u << cnt) - 1u));
+            const int m = a.sv.m;
+            if (k0 == 0) {  // empty segments before element 0
+              const int s0 = seg_of(a.sv, 0);
+              for (int q = 0; q < s0; q++) a.out[q] = Op::init();
+            }
+            while (ends) {
+              const int e = __ffs(ends) - 1;
+              ends &= ends - 1;
+              const unsigned hb = p_heads & ((2u << e) - 1u);  // heads up to e
+              const int ps0 = hb ? 31 - __clz((int)hb) : 0;
+              T pv2 = Op::ident();
+#pragma unroll
+              for (int i = 0; i < ITEMS; i++)
+                if (i >= ps0 && i <= e) pv2 = Op::apply(pv2, x[i]);
+              const int sg = seg_of(a.sv, k0 + e);
+              a.out[sg] = hb ? Op::apply(Op::init(), pv2) : Op::apply(run, pv2);
+              int s2 = sg + 1;  // empty segments that follow
+              while (s2 < m && __ldg(a.sv.off + s2 + 1) == k0 + e + 1) { a.out[s2] = Op::init(); ++s2; }
+            }
+          }
+        } else {
 #pragma unroll
         for (int i = 0; i < ITEMS; i++) {
           if ((p_heads >> i) & 1u) run = Op::init();
@@ -1061,6 +1097,7 @@ __global__ void __launch_bounds__(RTB, GCVL_RING_MINB)
         }
         fence_proxy_async_smem();
         named_arrive(3, RTB);  // outputs in the slot; the look-back warp stores them
+        }
       }
     } else if (prev >= 0) {
       // ------------------------------- look-back warp: store last round's tile
@@ -1069,9 +1106,11 @@ __global__ void __launch_bounds__(RTB, GCVL_RING_MINB)
       named_sync(3, RTB);
       if (lane == 0) {
         unsigned char *buf = ring + ps * TILE_BYTES;
-        tma_store_2d(&tout, buf, 0, prev * RTT);
-        bulk_commit();
-        bulk_wait_read_all();  // the slot is free once the store has read it
+        if constexpr (!RED) {
+          tma_store_2d(&tout, buf, 0, prev * RTT);
+          bulk_commit();
+          bulk_wait_read_all();  // the slot is free once the store has read it
+        }
         if (!mbar_wait(&bar[ps], (unsigned)((r - 1) / NB) & 1u, kRingDrain)) atomicOr(a.status, DEV_TIMEOUT);
         s_armed[ps] = r - 1 + NB;
         ring_arm(s_tile[ps], &bar[ps], buf, &tin, TILE_BYTES);
@@ -1225,17 +1264,18 @@ template <class T> constexpr size_t tma_smem(int wmax) {
 }
 
 // CTAs of a ring scan: as many as are resident at once (0: it does not fit)
-template <class Op, bool SEG> int ring_grid(int tiles) {
+template <class Op, bool SEG, bool RED = false> int ring_grid(int tiles) {
   static int per_sm = -1;
   if (per_sm < 0) {
     int nb = 0;
     const size_t smem = ring_smem<typename Op::T>();
     if (smem > 48 * 1024 &&
-        cudaFuncSetAttribute(k_scan_ring<Op, SEG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+        cudaFuncSetAttribute(k_scan_ring<Op, SEG, RED>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
             cudaSuccess) {
       cudaGetLastError();
       per_sm = 0;
-    } else if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_scan_ring<Op, SEG>, RTB, smem) != cudaSuccess) {
+    } else if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_scan_ring<Op, SEG, RED>, RTB, smem) !=
+               cudaSuccess) {
       cudaGetLastError();
       per_sm = 0;
     } else {
@@ -1271,6 +1311,28 @@ bool run_scan_tma(typename Op::T *out, const typename Op::T *in, vec_p sd, int n
       a.spin_limit = S.spin_limit;
       GCVL_CK(cudaMemsetAsync(mem, 0, lookback_clear_bytes(tiles), S.stream));
       k_scan_ring<Op, SEG><<<grid, RTB, ring_smem<T>(), S.stream>>>(tin, tout, a, tiles);
+      launch_check(name);
+      return true;
+    }
+  }
+  if constexpr (MODE == M_REDUCE && SEG && !std::is_same<Op, AddD>::value) {
+    // segmented reductions on the ring (results written at segment ends,
+    // the carry from the look-back: no fix-up pass)
+    const int tiles = ceil_div(n, (long)RTT * row_items<T>());
+    const int grid = ring_grid<Op, SEG, true>(tiles);
+    if (grid > 0) {
+      if (!tma_map<T>(&tin, in, rows, RTT)) return false;
+      void *mem = scratch_or_work(scratch, lookback_bytes(tiles));
+      if (!mem) return true;
+      TArgs<T> a{};
+      a.out = out; a.in = in; a.n = n; a.rows = rows;
+      a.sv = seg_view(sd, n, m);
+      a.lb = lookback_carve(mem, tiles);
+      a.status = S.d_status;
+      a.spin_limit = S.spin_limit;
+      // nothing runs on look-back words that were not cleared
+      if (!GCVL_CK(cudaMemsetAsync(mem, 0, lookback_clear_bytes(tiles), S.stream))) return true;
+      k_scan_ring<Op, SEG, true><<<grid, RTB, ring_smem<T>(), S.stream>>>(tin, tin, a, tiles);
       launch_check(name);
       return true;
     }
@@ -1464,7 +1526,10 @@ void run_reduce(const typename Op::T *in, int n, typename Op::T *result_dev, vec
 template <class T> int seg_reduce_units(int n) {
   if (n <= 0) return 0;
   const int a = ceil_div(n, tile_elems<T>()), b = ceil_div(n, TT * row_items<T>());
-  return (int)((reduce_pass_bytes(a > b ? a : b) + 7) / 8);
+  const size_t pass = reduce_pass_bytes(a > b ? a : b);
+  // the ring form (64-row tiles) needs only its look-back words
+  const size_t ring = lookback_bytes(ceil_div(n, (long)RTT * row_items<T>()));
+  return (int)(((pass > ring ? pass : ring) + 7) / 8);
 }
 template <class T> int reduce_units(int n) {
   (void)n;
