@@ -34,8 +34,6 @@ struct State {
   void *h_small = nullptr;          // 4 KB pinned host mirror
   void *work = nullptr;             // library workspace used when the caller
   size_t work_bytes = 0;            //   passes a NULL scratch vector
-  void *stage = nullptr;            // staging buffer for overlapping mov_fov
-  size_t stage_bytes = 0;
   uint64_t rand48 = 0;               // lrand48 state (glibc starts unseeded draws from 0)
   int spin_limit = 1 << 22;         // bounded-wait iteration limit
   int err = 0;

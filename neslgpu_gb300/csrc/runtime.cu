@@ -331,10 +331,67 @@ GCVL_EXPORT void fre_fov(vec_p p) {
   GCVL_CK(cudaFree(p));
 }
 
-// mov_fov must handle overlapping regions (facilt.c:162-183).  A plain
-// device copy is used when the ranges are disjoint; overlapping moves go
-// through a library staging buffer in pieces ordered so that no piece
-// overwrites source bytes that a later piece still reads.
+// mov_fov must handle overlapping regions (facilt.c:162-183).  Disjoint
+// regions take one device copy.  Overlapping ones take one cooperative
+// kernel that moves the region in rounds and allocates nothing: in each
+// round every CTA loads its part of the round's source units into
+// registers, all CTAs meet at a grid barrier, then store.  Moving down
+// (d < s) the rounds run from the front, moving up from the back; a round's
+// stores only overwrite source units that this or an earlier round has
+// already loaded, and the next round's loads do not touch what it stored,
+// so one barrier per round is enough.  The barrier's waits are bounded: a
+// round whose barrier gave up stores nothing and the timeout is reported.
+constexpr int MV_BLOCK = 256, MV_ITEMS = 16, MV_CHUNK = MV_BLOCK * MV_ITEMS;  // 8-byte units per CTA per round
+__device__ __forceinline__ bool grid_meet(unsigned *count, unsigned *gen, unsigned nblocks, unsigned *status,
+                                          int limit) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    const unsigned g = *(volatile unsigned *)gen;
+    __threadfence();
+    if (atomicAdd(count, 1u) == nblocks - 1) {
+      *(volatile unsigned *)count = 0;
+      __threadfence();
+      atomicAdd(gen, 1u);
+    } else {
+      int it = 0;
+      while (*(volatile unsigned *)gen == g) {
+        if (++it >= limit) { ok = 0; atomicOr(status, DEV_TIMEOUT); break; }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+__global__ void __launch_bounds__(MV_BLOCK) k_move_overlap(unsigned long long *d, const unsigned long long *s,
+                                                           long units, int up, unsigned *bar, unsigned *status,
+                                                           int limit) {
+  const long per_round = (long)gridDim.x * MV_CHUNK;
+  for (long r0 = 0; r0 < units; r0 += per_round) {
+    // this round covers [lo, lo + len) of the units, counted from the front
+    // (moving down) or from the back (moving up)
+    const long len = units - r0 < per_round ? units - r0 : per_round;
+    const long lo = up ? units - r0 - len : r0;
+    const long mine = lo + (long)blockIdx.x * MV_CHUNK;
+    unsigned long long v[MV_ITEMS];
+#pragma unroll
+    for (int c = 0; c < MV_ITEMS; c++) {
+      const long k = mine + c * MV_BLOCK + threadIdx.x;
+      if (k < lo + len) v[c] = s[k];
+    }
+    if (!grid_meet(bar, bar + 1, gridDim.x, status, limit)) return;
+#pragma unroll
+    for (int c = 0; c < MV_ITEMS; c++) {
+      const long k = mine + c * MV_BLOCK + threadIdx.x;
+      if (k < lo + len) d[k] = v[c];
+    }
+  }
+}
+
 GCVL_EXPORT void mov_fov(vec_p d, vec_p s, int size, vec_p scratch) {
   (void)scratch;
   ensure_init();
@@ -347,20 +404,30 @@ GCVL_EXPORT void mov_fov(vec_p d, vec_p s, int size, vec_p scratch) {
     GCVL_CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, S.stream));
     return;
   }
-  const size_t piece_max = (size_t)64 << 20;
-  if (!S.stage) {
-    if (!GCVL_CK(cudaMalloc(&S.stage, piece_max))) return;
-    S.stage_bytes = piece_max;
+  // every CTA of a cooperative launch is resident at once, so the grid
+  // barrier's waits end
+  static int per_sm = -1;
+  if (per_sm < 0) {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_move_overlap, MV_BLOCK, 0) != cudaSuccess ||
+        per_sm < 1) {
+      cudaGetLastError();
+      per_sm = 1;
+    }
   }
-  size_t done = 0;
-  while (done < bytes) {
-    size_t piece = bytes - done < piece_max ? bytes - done : piece_max;
-    // moving down: copy from the front; moving up: from the back
-    size_t at = dst < src ? done : bytes - done - piece;
-    GCVL_CK(cudaMemcpyAsync(S.stage, src + at, piece, cudaMemcpyDeviceToDevice, S.stream));
-    GCVL_CK(cudaMemcpyAsync(dst + at, S.stage, piece, cudaMemcpyDeviceToDevice, S.stream));
-    done += piece;
-  }
+  const long need = ((long)size + MV_CHUNK - 1) / MV_CHUNK;
+  const long cap = (long)per_sm * S.sm_count;
+  int grid = (int)(need < cap ? need : cap);
+  unsigned *bar = (unsigned *)((char *)S.d_small + 512);  // count, generation
+  if (!GCVL_CK(cudaMemsetAsync(bar, 0, 8, S.stream))) return;
+  unsigned long long *dp = (unsigned long long *)d;
+  const unsigned long long *sp = (const unsigned long long *)s;
+  long units = size;
+  int up = dst > src;
+  unsigned *status = S.d_status;
+  int limit = S.spin_limit;
+  void *args[] = {&dp, &sp, &units, &up, &bar, &status, &limit};
+  GCVL_CK(cudaLaunchCooperativeKernel((const void *)k_move_overlap, dim3(grid), dim3(MV_BLOCK), args, 0, S.stream));
+  launch_check("k_move_overlap");
 }
 GCVL_EXPORT int mov_fov_scratch(int size) { (void)size; return 0; }
 
