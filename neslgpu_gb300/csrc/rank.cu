@@ -617,14 +617,20 @@ __global__ void __launch_bounds__(WS_SCAN) k_ws_scan(unsigned *counts, int tiles
   }
 }
 
-template <bool POS>
+// VAL: each key's value (val[k]) moves with it to vout.  Dynamic shared
+// memory: ws_split_smem<V, VAL>() bytes.
+template <class V, bool VAL> constexpr size_t ws_split_smem() { return (size_t)WS_TILE * (4 + (VAL ? sizeof(V) : 0)); }
+template <bool POS, class V = unsigned, bool VAL = false>
 __global__ void __launch_bounds__(RK_BLOCK) k_window_split(const unsigned *__restrict__ key, long n, int shift,
                                                            int nw, const unsigned *__restrict__ first,
                                                            const unsigned *gate, unsigned *__restrict__ kout,
-                                                           unsigned *__restrict__ pos) {
+                                                           unsigned *__restrict__ pos, const V *__restrict__ val = nullptr,
+                                                           V *__restrict__ vout = nullptr) {
   __shared__ unsigned s_cnt[WS_MAXW];   // the tile's count per window, then its first slot there in the tile
   __shared__ unsigned s_base[WS_MAXW];  // global slot of the window's first key of this tile
-  __shared__ unsigned s_key[WS_TILE];
+  extern __shared__ __align__(16) unsigned char rk_smem[];
+  unsigned *s_key = (unsigned *)rk_smem;                  // [WS_TILE] keys by window
+  V *s_val = (V *)(rk_smem + (size_t)WS_TILE * 4);        // [WS_TILE] their values (VAL)
   __shared__ unsigned s_ws[RK_WARPS];
   if (!*(const volatile unsigned *)gate) return;  // the same answer for every CTA
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -635,10 +641,14 @@ __global__ void __launch_bounds__(RK_BLOCK) k_window_split(const unsigned *__res
   const long base = (long)t * WS_TILE;
   const int valid = (int)min((long)WS_TILE, n - base);
   unsigned k[WS_ITEMS], r[WS_ITEMS];
+  V v[VAL ? WS_ITEMS : 1];
 #pragma unroll
   for (int c = 0; c < WS_ITEMS; c++) {
     const int e = c * RK_BLOCK + tid;
-    if (e < valid) k[c] = __ldcs(key + base + e);
+    if (e < valid) {
+      k[c] = __ldcs(key + base + e);
+      if constexpr (VAL) v[c] = __ldcs(val + base + e);
+    }
   }
 #pragma unroll
   for (int c = 0; c < WS_ITEMS; c++)
@@ -665,6 +675,7 @@ __global__ void __launch_bounds__(RK_BLOCK) k_window_split(const unsigned *__res
     if (e < valid) {
       const unsigned w = ws_window(k[c], shift, nw);
       s_key[s_cnt[w] + r[c]] = k[c];
+      if constexpr (VAL) s_val[s_cnt[w] + r[c]] = v[c];
       if (POS) pos[base + e] = s_base[w] + r[c];
     }
   }
@@ -674,7 +685,9 @@ __global__ void __launch_bounds__(RK_BLOCK) k_window_split(const unsigned *__res
   for (int e = tid; e < valid; e += RK_BLOCK) {
     const unsigned kk = s_key[e];
     const unsigned w = ws_window(kk, shift, nw);
-    kout[s_base[w] + (unsigned)e - s_cnt[w]] = kk;
+    const unsigned g = s_base[w] + (unsigned)e - s_cnt[w];
+    kout[g] = kk;
+    if constexpr (VAL) vout[g] = s_val[e];
   }
 }
 
@@ -764,23 +777,37 @@ inline size_t rk_state_bytes(long n) { return (size_t)rk_tiles(n) * 256 * 4; }
 inline int window_shift(int n) { int b = bit_length((unsigned)(n > 1 ? n - 1 : 1)); return b > 8 ? b - 8 : 0; }
 
 // ------------------------------------------------ partitioned scatter ---
-// d[idx[k]] = s[k] for k < n (idx in [0, n_d)): partition (idx, value) by
-// the top 8 bits of the index, then scatter window by window.
-struct ScatterLayout { size_t kout, vout, hist, counter, state, total; };
+// d[idx[k]] = s[k] for k < n (idx in [0, n_d)) when d is larger than L2 can
+// absorb random writes to (each would cost a DRAM read-modify-write of a
+// sector): the (index, value) pairs are split by destination window (windows
+// of about 32 MB, at most 256, with the same histogram, scan and split passes
+// as the partitioned gather), then written window by window while each window
+// sits in L2.  Ascending indices take one streaming scatter instead; the
+// device decides (the kernels of the branch not taken return at once).
+struct ScatterLayout { size_t kout, vout, counts, totals, flags, total; };
 inline ScatterLayout scatter_layout(long n, size_t vsize) {
   ScatterLayout L;
   size_t o = 0;
   auto take = [&](size_t bytes) { size_t at = o; o += align_up(bytes, 256); return at; };
   L.kout = take((size_t)n * 4);
   L.vout = take((size_t)n * vsize);
-  L.hist = take(256 * 4);
-  L.counter = take(256);
-  L.state = take(rk_state_bytes(n));
+  L.counts = take((size_t)rk_tiles(n) * WS_MAXW * 4);
+  L.totals = take(WS_MAXW * 4);
+  L.flags = take(256);
   L.total = o + 256;  // room to align the base
   return L;
 }
 bool scatter_partitioned_wanted(long n_d, size_t vsize) { return (size_t)n_d * vsize > (size_t)RK_DIRECT_MAX * 4; }
 size_t scatter_partitioned_bytes(long n, size_t vsize) { return scatter_layout(n, vsize).total; }
+// windows of about 32 MB of `bytes`, a power of two from 2 to 256: (log2 of
+// the count, shift of an index of [0, len) to its window)
+inline void ws_windows(size_t bytes, long len, int *wbits, int *shift) {
+  int wb = 1;
+  while (wb < 8 && (bytes >> wb) > ((size_t)32 << 20)) ++wb;
+  const int nb = bit_length((unsigned)(len > 1 ? len - 1 : 1));
+  *wbits = wb;
+  *shift = nb > wb ? nb - wb : 0;
+}
 
 template <class V>
 void scatter_partitioned(V *d, const V *s, const int *idx, int n, int n_d, vec_p scratch) {
@@ -790,34 +817,35 @@ void scatter_partitioned(V *d, const V *s, const int *idx, int n, int n_d, vec_p
   char *raw = (char *)scratch_or_work(scratch, L.total);
   if (!raw) return;
   char *mem = (char *)align_up((size_t)raw, 256);
-  unsigned *hist = (unsigned *)(mem + L.hist);
-  unsigned *counter = (unsigned *)(mem + L.counter);
-  unsigned *state = (unsigned *)(mem + L.state);
-  const int shift = window_shift(n_d);
+  unsigned *kout = (unsigned *)(mem + L.kout);
+  V *vout = (V *)(mem + L.vout);
+  unsigned *counts = (unsigned *)(mem + L.counts);
+  unsigned *totals = (unsigned *)(mem + L.totals);
+  unsigned *unsorted = (unsigned *)(mem + L.flags);  // the gate: non-zero when some index exceeds its successor
+  int wbits, shift;
+  ws_windows((size_t)n_d * sizeof(V), n_d, &wbits, &shift);
+  const int nw = 1 << wbits;
   const int tiles = rk_tiles(n);
-  unsigned *unsorted = counter + 1;  // the gate: non-zero when some index exceeds its successor
-  GCVL_CK(cudaMemsetAsync(hist, 0, 256 * 4, S.stream));
-  GCVL_CK(cudaMemsetAsync(counter, 0, 8, S.stream));
-  GCVL_CK(cudaMemsetAsync(state, 0, rk_state_bytes(n), S.stream));
-  int hg = S.sm_count * 4;
-  if ((long)hg * RK_BLOCK > n) hg = (n + RK_BLOCK - 1) / RK_BLOCK;
-  k_digit_hist<<<hg, RK_BLOCK, 0, S.stream>>>((const unsigned *)idx, n, shift, hist, unsorted);
-  launch_check("k_digit_hist");
-  k_rank_digit_starts<<<1, 256, 0, S.stream>>>(hist, 1);
-  launch_check("k_rank_digit_starts");
-  // ascending indices (e.g. an interleave): one streaming scatter; otherwise
-  // partition by window, then scatter window by window.  The device decides:
-  // the kernels of the branch not taken return at once.
-  const int g = sc_grid(n);
-  k_sorted_scatter<V><<<g, RK_BLOCK, 0, S.stream>>>(d, s, idx, n, unsorted);
+  constexpr size_t smem = ws_split_smem<V, true>();
+  static bool attr = false;
+  if (!attr) {
+    GCVL_CK(cudaFuncSetAttribute(k_window_split<false, V, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem));
+    attr = true;
+  }
+  if (!GCVL_CK(cudaMemsetAsync(unsorted, 0, 4, S.stream))) return;
+  k_ws_hist<<<tiles, RK_BLOCK, 0, S.stream>>>((const unsigned *)idx, n, shift, nw, counts, unsorted);
+  launch_check("k_ws_hist");
+  k_sorted_scatter<V><<<sc_grid(n), RK_BLOCK, 0, S.stream>>>(d, s, idx, n, unsorted);
   launch_check("k_sorted_scatter");
-  PassArgs<unsigned, V> a{};
-  a.kin = (const unsigned *)idx; a.vin = s;
-  a.kout = (unsigned *)(mem + L.kout); a.vout = (V *)(mem + L.vout);
-  a.starts = hist; a.state = state; a.counter = counter; a.gate = unsorted;
-  a.n = n; a.shift = shift; a.status = S.d_status; a.spin_limit = S.spin_limit;
-  launch_pass<unsigned, V, false, IN_ARRAYS, OUT_ARRAYS, false>(a, tiles);
-  k_window_scatter<V><<<sc_blocks(n), RK_BLOCK, 0, S.stream>>>(d, a.kout, a.vout, n, unsorted);
+  k_ws_totals<<<nw, RK_BLOCK, 0, S.stream>>>(counts, tiles, totals, unsorted);
+  launch_check("k_ws_totals");
+  k_ws_scan<<<nw, WS_SCAN, 0, S.stream>>>(counts, tiles, nw, totals, unsorted);
+  launch_check("k_ws_scan");
+  k_window_split<false, V, true><<<tiles, RK_BLOCK, smem, S.stream>>>((const unsigned *)idx, n, shift, nw, counts,
+                                                                      unsorted, kout, nullptr, s, vout);
+  launch_check("k_window_split");
+  k_window_scatter<V><<<sc_blocks(n), RK_BLOCK, 0, S.stream>>>(d, kout, vout, n, unsorted);
   launch_check("k_window_scatter");
 }
 
@@ -865,12 +893,8 @@ void gather_partitioned(V *d, const V *s, const int *idx, int n, int n_src, vec_
   unsigned *counts = (unsigned *)(mem + L.counts);
   unsigned *totals = (unsigned *)(mem + L.totals);
   unsigned *unsorted = (unsigned *)(mem + L.flags);  // the gate: non-zero when some index exceeds its successor
-  // windows of about 32 MB of the source, a power of two from 2 to 256
-  const size_t src_bytes = (size_t)n_src * sizeof(V);
-  int wbits = 1;
-  while (wbits < 8 && (src_bytes >> wbits) > ((size_t)32 << 20)) ++wbits;
-  const int nb = bit_length((unsigned)(n_src > 1 ? n_src - 1 : 1));
-  const int shift = nb > wbits ? nb - wbits : 0;
+  int wbits, shift;
+  ws_windows((size_t)n_src * sizeof(V), n_src, &wbits, &shift);
   const int nw = 1 << wbits;
   const int tiles = rk_tiles(n);
   GCVL_CK(cudaMemsetAsync(unsorted, 0, 4, S.stream));
@@ -882,8 +906,8 @@ void gather_partitioned(V *d, const V *s, const int *idx, int n, int n_src, vec_
   launch_check("k_ws_totals");
   k_ws_scan<<<nw, WS_SCAN, 0, S.stream>>>(counts, tiles, nw, totals, unsorted);
   launch_check("k_ws_scan");
-  k_window_split<true><<<tiles, RK_BLOCK, 0, S.stream>>>((const unsigned *)idx, n, shift, nw, counts, unsorted,
-                                                         kout, pos);
+  k_window_split<true><<<tiles, RK_BLOCK, ws_split_smem<unsigned, false>(), S.stream>>>(
+      (const unsigned *)idx, n, shift, nw, counts, unsorted, kout, pos);
   launch_check("k_window_split");
   k_window_gather<V><<<sc_blocks(n), RK_BLOCK, 0, S.stream>>>(p, s, kout, n, (unsigned)n_src, unsorted,
                                                               S.d_status);
