@@ -364,7 +364,32 @@ def batched_suite(g, nvec=8192, total=1 << 27, seed=3):
     res["graph_gelem_s"] = round(res["elements"] / (res["graph_ms"] * 1e-3) / 1e9, 2)
     res["speedup_batched_vs_percall"] = round(res["percall_ms"] / res["batched_ms"], 2)
     res["speedup_graph_vs_percall"] = round(res["percall_ms"] / res["graph_ms"], 2)
+    res["skewed"] = skewed_batch_suite(g)
     return res
+
+
+def skewed_batch_suite(g):
+    """Flattening's worst case: 4 vectors of 2^24 elements beside 8188 of
+    1-100 elements, against one vector of the same total length (the same
+    bytes with no vector boundaries: the bound for any launch scheme,
+    a persistent (vector, op) queue included).  int32 and float64."""
+    from neslgpu_gb300 import batch as B
+    out = {}
+    for dbl in (False, True):
+        sk = B.make_skewed_batch()
+        row = {"vectors": sk.nvec, "elements": sk.n}
+        for name, b, modes in (("skewed", sk, ("percall", "batched", "graph")),
+                               ("one_vector", B.single_vector_batch(sk.n), ("batched", "graph"))):
+            run = B.BatchRun(b, dbl, cvl=g.c)
+            try:
+                for mode in modes:
+                    row[f"{name}_{mode}_ms"] = round(run.timeit(mode, reps=3 if mode == "percall" else 10) * 1e3, 3)
+            finally:
+                run.free()
+        row["batched_vs_one_vector"] = round(row["skewed_batched_ms"] / row["one_vector_batched_ms"], 3)
+        row["graph_vs_one_vector"] = round(row["skewed_graph_ms"] / row["one_vector_graph_ms"], 3)
+        out["float64" if dbl else "int32"] = row
+    return out
 
 
 def dispatch_suite(g, count=512, hi=24, seed=2024):
@@ -496,42 +521,12 @@ def graph_suite(c, sync, seed=7):
     return out
 
 
-def vinterp_suite(g, log2n=26, log2rows=22, seed=2026, cpu_sample_log2n=20):
-    """The plain drop-in at scale through a VCODE interpreter: NESL
-    quicksort (this repository's flattened VCODE program) on 2^log2n
-    uniform int32 keys, and sparse matrix-vector product as a VCODE
-    program on 2^log2rows rows with power-law row lengths (alpha 2.1 on
-    [1, 2^16]), float64 values and x."""
+def _spmv_case(g, rows, r, sync):
+    """CSR SpMV through the VCODE program and through the fused kernel on
+    `rows` rows with power-law row lengths (alpha 2.1 on [1, 2^16]), column
+    indices uniform, float64 N(0,1) values and x."""
     from neslgpu_gb300 import vcode as V, vcode_programs as P
     c = g.c
-    sync = lambda: c.gcvl_sync()  # noqa: E731
-    r = np.random.default_rng(seed)
-    n = 1 << log2n
-    keys = r.integers(-2 ** 31, 2 ** 31, size=n, dtype=np.int64).astype(np.int32)
-    _vcode_sort(c, keys[: 1 << 16], sync)  # warm-up: kernels loaded, heap classes touched
-    dev_s, e2e_s, out, ops = _vcode_sort(c, keys, sync)
-    ok = bool(np.all(out[1:] >= out[:-1])) and int(out.astype(np.int64).sum()) == int(keys.astype(np.int64).sum())
-    qs = {"n": n, "keys": "uniform int32, seeded", "seconds": round(dev_s, 4),
-          "mkeys_s": round(n / dev_s / 1e6, 2), "e2e_seconds": round(e2e_s, 4),
-          "e2e_mkeys_s": round(n / e2e_s / 1e6, 2), "vcode_ops": ops, "sorted": ok}
-    # the .fcode form: elementwise chains as generated fused kernels
-    from neslgpu_gb300 import fcode as F, vcode_programs as P
-    lib = F.FusedLib(P.qsort_fcode_program()[1])
-    _vcode_sort(c, keys[: 1 << 16], sync, lib)
-    fdev, fe2e, fout, fops = _vcode_sort(c, keys, sync, lib)
-    qs["fcode"] = {"seconds": round(fdev, 4), "mkeys_s": round(n / fdev / 1e6, 2), "vcode_ops": fops,
-                   "same_result": bool(np.array_equal(fout, out)), "speedup_vs_vcode": round(dev_s / fdev, 3)}
-    if cpu_sample_log2n:
-        # the same interpreter and program on the oracle's serial CVL
-        # restatement, one host thread, on a bounded sample
-        from oracle.oracle import load_oracle
-        ns = 1 << cpu_sample_log2n
-        cs, _, cout, _ = _vcode_sort(load_oracle(), keys[:ns], lambda: None)
-        qs["cpu_baseline"] = {"mkeys_s": round(ns / cs / 1e6, 3), "n": ns, "cores": 1, "kind": "port",
-                              "sample": f"the first 2^{cpu_sample_log2n} keys, same VCODE program, oracle CVL",
-                              "sorted": bool(np.all(cout[1:] >= cout[:-1]))}
-    # sparse matrix-vector product
-    rows = 1 << log2rows
     lens = np.minimum(r.zipf(2.1, size=rows), 1 << 16).astype(np.int32)
     nnz = int(lens.sum(dtype=np.int64))
     cols = r.integers(0, rows, size=nnz).astype(np.int32)
@@ -596,6 +591,49 @@ def vinterp_suite(g, log2n=26, log2rows=22, seed=2026, cpu_sample_log2n=20):
                       "alg_gbs": round((nnz * (4 + 8 + 8) + 8 * rows + 4 * rows) / tf / 1e9, 1),
                       "speedup_vs_vcode": round(t / tf, 2),
                       "max_abs_diff_vs_vcode": float(np.max(np.abs(yf - yh)))}}
+    return spmv
+
+
+def vinterp_suite(g, log2n=26, log2rows=22, seed=2026, cpu_sample_log2n=20):
+    """The plain drop-in at scale through a VCODE interpreter: NESL
+    quicksort (this repository's flattened VCODE program) on 2^log2n
+    uniform int32 keys, and sparse matrix-vector product as a VCODE
+    program on 2^log2rows rows with power-law row lengths (alpha 2.1 on
+    [1, 2^16]), float64 values and x -- about 2^24.2 nonzeros at 2^22 rows,
+    so the same law on 8x the rows ("row_scaled") brings it to about 2^27."""
+    from neslgpu_gb300 import vcode as V, vcode_programs as P
+    c = g.c
+    sync = lambda: c.gcvl_sync()  # noqa: E731
+    r = np.random.default_rng(seed)
+    n = 1 << log2n
+    keys = r.integers(-2 ** 31, 2 ** 31, size=n, dtype=np.int64).astype(np.int32)
+    _vcode_sort(c, keys[: 1 << 16], sync)  # warm-up: kernels loaded, heap classes touched
+    dev_s, e2e_s, out, ops = _vcode_sort(c, keys, sync)
+    ok = bool(np.all(out[1:] >= out[:-1])) and int(out.astype(np.int64).sum()) == int(keys.astype(np.int64).sum())
+    qs = {"n": n, "keys": "uniform int32, seeded", "seconds": round(dev_s, 4),
+          "mkeys_s": round(n / dev_s / 1e6, 2), "e2e_seconds": round(e2e_s, 4),
+          "e2e_mkeys_s": round(n / e2e_s / 1e6, 2), "vcode_ops": ops, "sorted": ok}
+    # the .fcode form: elementwise chains as generated fused kernels
+    from neslgpu_gb300 import fcode as F, vcode_programs as P
+    lib = F.FusedLib(P.qsort_fcode_program()[1])
+    _vcode_sort(c, keys[: 1 << 16], sync, lib)
+    fdev, fe2e, fout, fops = _vcode_sort(c, keys, sync, lib)
+    qs["fcode"] = {"seconds": round(fdev, 4), "mkeys_s": round(n / fdev / 1e6, 2), "vcode_ops": fops,
+                   "same_result": bool(np.array_equal(fout, out)), "speedup_vs_vcode": round(dev_s / fdev, 3)}
+    if cpu_sample_log2n:
+        # the same interpreter and program on the oracle's serial CVL
+        # restatement, one host thread, on a bounded sample
+        from oracle.oracle import load_oracle
+        ns = 1 << cpu_sample_log2n
+        cs, _, cout, _ = _vcode_sort(load_oracle(), keys[:ns], lambda: None)
+        qs["cpu_baseline"] = {"mkeys_s": round(ns / cs / 1e6, 3), "n": ns, "cores": 1, "kind": "port",
+                              "sample": f"the first 2^{cpu_sample_log2n} keys, same VCODE program, oracle CVL",
+                              "sorted": bool(np.all(cout[1:] >= cout[:-1]))}
+    # sparse matrix-vector product: the configured 2^log2rows rows (about
+    # 2^24.2 nonzeros), and the same row-length law on 8x the rows, which
+    # reaches about 2^27 nonzeros
+    spmv = _spmv_case(g, 1 << log2rows, r, sync)
+    spmv["row_scaled"] = _spmv_case(g, 8 << log2rows, r, sync)
     return {"quicksort": qs, "spmv": spmv, "graph": graph_suite(c, sync)}
 
 

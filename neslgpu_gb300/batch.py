@@ -53,6 +53,29 @@ def make_batch(nvec: int, total: int, seed: int = 3, lo: int = 10, hi: int = 10 
     r = W.rng(seed)
     raw = np.clip(np.exp(r.normal(np.log(np.sqrt(lo * hi)), 1.6, size=nvec)), lo, hi)
     vl = np.clip(np.rint(raw * (total / raw.sum())), lo, hi).astype(np.int64)
+    return batch_from_lengths(vl, r, inner_mean)
+
+
+def make_skewed_batch(huge: int = 4, huge_len: int = 1 << 24, tiny: int = 8188, tiny_hi: int = 100,
+                      seed: int = 5, inner_mean: float = 32.0) -> BatchData:
+    """The flattened form's worst case: a few huge vectors beside thousands
+    of tiny ones (lengths log-uniform in [1, tiny_hi]), the huge ones spread
+    among the tiny."""
+    r = W.rng(seed)
+    small = np.rint(np.exp(r.uniform(0.0, np.log(tiny_hi), size=tiny))).astype(np.int64)
+    vl = np.concatenate([np.full(huge, huge_len, dtype=np.int64), np.maximum(small, 1)])
+    return batch_from_lengths(vl[r.permutation(vl.size)], r, inner_mean)
+
+
+def single_vector_batch(total: int, seed: int = 6, inner_mean: float = 32.0) -> BatchData:
+    """One vector of `total` elements: the same work with no vector
+    boundaries, which no launch scheme over the same bytes can beat."""
+    return batch_from_lengths(np.array([total], dtype=np.int64), W.rng(seed), inner_mean)
+
+
+def batch_from_lengths(vl: np.ndarray, r, inner_mean: float = 32.0) -> BatchData:
+    """Vectors of the given lengths, inner segments geometric with `inner_mean`."""
+    nvec = int(vl.size)
     segs, nseg = [], []
     for L in vl:
         s = W.geometric_lengths(r, int(L), inner_mean)

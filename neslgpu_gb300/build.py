@@ -40,17 +40,28 @@ def _stale(target: Path, deps: list[Path]) -> bool:
     return any(d.stat().st_mtime > t for d in deps)
 
 
+def tuning_defines() -> list[str]:
+    """-D flags for the kernels' tuning macros (GCVL_RK_ITEMS, GCVL_RING_MINB,
+    ...) from GCVL_TUNE="NAME=VALUE ...": for timing other tile and
+    occupancy choices than the defaults in the sources."""
+    return [f"-D{x}" for x in os.environ.get("GCVL_TUNE", "").split() if x.startswith("GCVL_")]
+
+
 def build_library(verbose: bool = False, force: bool = False) -> Path:
     BUILD.mkdir(exist_ok=True)
     sources = sorted(CSRC.glob("*.cu"))
     headers = sorted(CSRC.glob("*.cuh")) + sorted((ROOT / "include").glob("*.h"))
+    tune = tuning_defines()
+    stamp = BUILD / "tuning"
+    if (stamp.read_text() if stamp.exists() else "") != " ".join(tune):
+        force = True  # objects built with other tuning macros
     objs = []
     jobs = []
     for src in sources:
         obj = BUILD / (src.stem + ".o")
         objs.append(obj)
         if force or _stale(obj, [src, *headers, Path(__file__)]):
-            jobs.append([nvcc(), *ARCH, *NVCC_FLAGS, "-c", str(src), "-o", str(obj)])
+            jobs.append([nvcc(), *ARCH, *NVCC_FLAGS, *tune, "-c", str(src), "-o", str(obj)])
 
     def run(cmd):
         if verbose:
@@ -68,6 +79,7 @@ def build_library(verbose: bool = False, force: bool = False) -> Path:
     if force or jobs or _stale(LIB, objs):
         cmd = [nvcc(), *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-ldl"]
         run(cmd)
+    stamp.write_text(" ".join(tune))
     return LIB
 
 

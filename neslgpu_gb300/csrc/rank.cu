@@ -508,36 +508,80 @@ __global__ void __launch_bounds__(RK_BLOCK) k_window_scatter(V *__restrict__ d, 
 // ------------------------------------------------------ window split ---
 // Groups keys by window (key >> shift, clamped below nw: the same function in
 // every pass) without any tile waiting on another: a histogram pass writes
-// each tile's per-window counts (window-major), a scan turns them into every
-// (window, tile)'s first slot, and the split pass places each tile's keys
-// there.  Slots within a window and tile come from shared-memory atomics (no
+// each tile's per-window counts (window-major), their exclusive scan (the
+// library's int +-scan, in place) is every (window, tile)'s first slot --
+// the windows before w, then the tiles before t -- and the split pass
+// places each tile's keys there.  Slots within a window and tile come from shared-memory atomics (no
 // particular order); the tile is staged in shared memory by window and each
 // window's run leaves as one coalesced run; with POS, pos[k] = the slot key
 // k went to, written in the input order.  The partitioned gather uses it.
 constexpr int WS_ITEMS = 16, WS_TILE = RK_BLOCK * WS_ITEMS, WS_MAXW = 256;
 __device__ __forceinline__ unsigned ws_window(unsigned k, int shift, int nw) { return min(k >> shift, (unsigned)(nw - 1)); }
+// this key's slot among the keys of window w counted in cnt[w] so far (w <
+// 0: none).  One shared-memory atomic per key: a per-warp form (lanes of
+// one window found by a ballot per window bit, one atomic per window) made
+// the partitioned gather and scatter 1.4-1.6x slower.
+__device__ __forceinline__ unsigned ws_slot(unsigned *cnt, int w) { return w >= 0 ? atomicAdd(cnt + w, 1u) : 0u; }
 
 // counts[w * tiles + t] = keys of tile t in window w; *unsorted != 0 when
-// some key exceeds its successor
-__global__ void __launch_bounds__(RK_BLOCK) k_ws_hist(const unsigned *__restrict__ key, long n, int shift, int nw,
+// some key exceeds its successor.  VEC: key is 16-byte aligned, and each
+// thread reads four keys at a time.
+template <bool VEC>
+__global__ void __launch_bounds__(RK_BLOCK) k_ws_hist(const unsigned *__restrict__ key, long n, int shift, int wbits,
                                                       unsigned *__restrict__ counts, unsigned *unsorted) {
   __shared__ unsigned s_cnt[WS_MAXW];
   __shared__ int s_uns;
-  const int tid = threadIdx.x;
+  const int tid = threadIdx.x, nw = 1 << wbits;
   const int tiles = gridDim.x, t = blockIdx.x;
   s_cnt[tid] = 0;
   if (tid == 0) s_uns = 0;
   __syncthreads();
   const long base = (long)t * WS_TILE;
   int uns = 0;
-#pragma unroll 4
-  for (int c = 0; c < WS_ITEMS; c++) {
-    const long e = base + c * RK_BLOCK + tid;
-    if (e < n) {
-      const unsigned k = __ldcs(key + e);
-      atomicAdd(&s_cnt[ws_window(k, shift, nw)], 1u);
+  if constexpr (VEC) {
+    uint4 q[WS_ITEMS / 4];
+    unsigned nx[WS_ITEMS / 4];
+#pragma unroll
+    for (int c = 0; c < WS_ITEMS / 4; c++) {
+      const long e = base + 4L * (c * RK_BLOCK + tid);
+      q[c] = make_uint4(0, 0, 0, 0);
+      nx[c] = 0xFFFFFFFFu;
+      if (e + 3 < n) {
+        q[c] = __ldcs(reinterpret_cast<const uint4 *>(key + e));
+        // the successor of the fourth key: the next lane's line, just read
+        if (e + 4 < n) nx[c] = __ldg(key + e + 4);
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < WS_ITEMS / 4; c++) {
+      const long e = base + 4L * (c * RK_BLOCK + tid);
+      const unsigned k4[4] = {q[c].x, q[c].y, q[c].z, q[c].w};
+      if (e + 3 < n) {
+        if (k4[0] > k4[1] || k4[1] > k4[2] || k4[2] > k4[3] || k4[3] > nx[c]) uns = 1;
+      } else {
+        for (int u = 0; u < 4; u++)  // the vector's ragged end
+          if (e + u + 1 < n && __ldg(key + e + u) > __ldg(key + e + u + 1)) uns = 1;
+      }
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        int w = -1;
+        if (e + u < n) w = (int)ws_window(e + 3 < n ? k4[u] : __ldg(key + e + u), shift, nw);
+        ws_slot(s_cnt, w);
+      }
+    }
+  } else {
+    unsigned k[WS_ITEMS];
+#pragma unroll
+    for (int c = 0; c < WS_ITEMS; c++) {
+      const long e = base + c * RK_BLOCK + tid;
+      k[c] = e < n ? __ldcs(key + e) : 0u;
+    }
+#pragma unroll
+    for (int c = 0; c < WS_ITEMS; c++) {
+      const long e = base + c * RK_BLOCK + tid;
       // the successor's load usually hits the line just read by the next lane
-      if (e + 1 < n && k > __ldg(key + e + 1)) uns = 1;
+      if (e + 1 < n && k[c] > __ldg(key + e + 1)) uns = 1;
+      ws_slot(s_cnt, e < n ? (int)ws_window(k[c], shift, nw) : -1);
     }
   }
   if (__any_sync(0xffffffffu, uns) && (tid & 31) == 0) s_uns = 1;
@@ -546,83 +590,12 @@ __global__ void __launch_bounds__(RK_BLOCK) k_ws_hist(const unsigned *__restrict
   if (tid == 0 && s_uns) atomicOr(unsorted, 1u);
 }
 
-// one CTA per window: totals[w] = its count over all tiles
-__global__ void __launch_bounds__(RK_BLOCK) k_ws_totals(const unsigned *__restrict__ counts, int tiles,
-                                                        unsigned *__restrict__ totals, const unsigned *gate) {
-  __shared__ unsigned s_ws[RK_WARPS];
-  if (!*(const volatile unsigned *)gate) return;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, w = blockIdx.x;
-  unsigned sum = 0;
-  for (int t = tid; t < tiles; t += RK_BLOCK) sum += __ldg(counts + (long)w * tiles + t);
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
-  if (lane == 0) s_ws[warp] = sum;
-  __syncthreads();
-  if (tid == 0) {
-    unsigned tot = 0;
-#pragma unroll
-    for (int q = 0; q < RK_WARPS; q++) tot += s_ws[q];
-    totals[w] = tot;
-  }
-}
-
-// one CTA of WS_SCAN threads per window: counts[w][t] -> the first slot of
-// (w, t): the windows before w, then the tiles before t.  Each thread takes
-// WS_SCAN_ITEMS consecutive tiles at a time with all its loads in flight.
-constexpr int WS_SCAN = 1024, WS_SCAN_ITEMS = 8;
-__global__ void __launch_bounds__(WS_SCAN) k_ws_scan(unsigned *counts, int tiles, int nw,
-                                                     const unsigned *__restrict__ totals, const unsigned *gate) {
-  __shared__ unsigned s_ws[WS_SCAN / 32];
-  __shared__ unsigned s_start;
-  if (!*(const volatile unsigned *)gate) return;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, w = blockIdx.x;
-  if (tid == 0) {
-    unsigned st0 = 0;
-    for (int q = 0; q < w; q++) st0 += __ldg(totals + q);
-    s_start = st0;
-  }
-  unsigned *row = counts + (long)w * tiles;
-  __syncthreads();
-  unsigned carry = s_start;
-  for (int t0 = 0; t0 < tiles; t0 += WS_SCAN * WS_SCAN_ITEMS) {
-    const int tb = t0 + tid * WS_SCAN_ITEMS;
-    unsigned c[WS_SCAN_ITEMS];
-    unsigned sum = 0;
-#pragma unroll
-    for (int q = 0; q < WS_SCAN_ITEMS; q++) {
-      c[q] = tb + q < tiles ? row[tb + q] : 0u;
-      sum += c[q];
-    }
-    unsigned incl = sum;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const unsigned x = shfl_up(incl, o);
-      if (lane >= o) incl += x;
-    }
-    if (lane == 31) s_ws[warp] = incl;
-    __syncthreads();
-    unsigned run = carry + incl - sum, all = 0;
-#pragma unroll 4
-    for (int q = 0; q < WS_SCAN / 32; q++) {
-      if (q < warp) run += s_ws[q];
-      all += s_ws[q];
-    }
-#pragma unroll
-    for (int q = 0; q < WS_SCAN_ITEMS; q++) {
-      if (tb + q < tiles) row[tb + q] = run;
-      run += c[q];
-    }
-    carry += all;
-    __syncthreads();  // s_ws is reused by the next chunk
-  }
-}
-
 // VAL: each key's value (val[k]) moves with it to vout.  Dynamic shared
 // memory: ws_split_smem<V, VAL>() bytes.
 template <class V, bool VAL> constexpr size_t ws_split_smem() { return (size_t)WS_TILE * (4 + (VAL ? sizeof(V) : 0)); }
 template <bool POS, class V = unsigned, bool VAL = false>
 __global__ void __launch_bounds__(RK_BLOCK) k_window_split(const unsigned *__restrict__ key, long n, int shift,
-                                                           int nw, const unsigned *__restrict__ first,
+                                                           int wbits, const unsigned *__restrict__ first,
                                                            const unsigned *gate, unsigned *__restrict__ kout,
                                                            unsigned *__restrict__ pos, const V *__restrict__ val = nullptr,
                                                            V *__restrict__ vout = nullptr) {
@@ -633,7 +606,7 @@ __global__ void __launch_bounds__(RK_BLOCK) k_window_split(const unsigned *__res
   V *s_val = (V *)(rk_smem + (size_t)WS_TILE * 4);        // [WS_TILE] their values (VAL)
   __shared__ unsigned s_ws[RK_WARPS];
   if (!*(const volatile unsigned *)gate) return;  // the same answer for every CTA
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = 1 << wbits;
   const int tiles = gridDim.x, t = blockIdx.x;
   s_cnt[tid] = 0;
   if (tid < nw) s_base[tid] = __ldg(first + (long)tid * tiles + t);
@@ -652,7 +625,7 @@ __global__ void __launch_bounds__(RK_BLOCK) k_window_split(const unsigned *__res
   }
 #pragma unroll
   for (int c = 0; c < WS_ITEMS; c++)
-    if (c * RK_BLOCK + tid < valid) r[c] = atomicAdd(&s_cnt[ws_window(k[c], shift, nw)], 1u);
+    r[c] = ws_slot(s_cnt, c * RK_BLOCK + tid < valid ? (int)ws_window(k[c], shift, nw) : -1);
   __syncthreads();
   // the windows' first slots within the tile: exclusive scan over the bins
   const unsigned tot = s_cnt[tid];
@@ -731,21 +704,25 @@ __global__ void __launch_bounds__(RK_BLOCK) k_gather_gated(V *__restrict__ d, co
                                                            const unsigned *__restrict__ idx, long n,
                                                            const unsigned *gate, int when_set) {
   if ((*(const volatile unsigned *)gate != 0) != (when_set != 0)) return;
-  const long i0 = (long)blockIdx.x * (RK_BLOCK * SC_ITEMS) + threadIdx.x;
-  unsigned k[SC_ITEMS];
-  V v[SC_ITEMS];
+  // grid-stride: launched with one CTA per 2048 elements it makes one pass;
+  // launched with few CTAs it costs little when the gate turns it away
+  for (long i0 = (long)blockIdx.x * (RK_BLOCK * SC_ITEMS) + threadIdx.x; i0 < n;
+       i0 += (long)gridDim.x * (RK_BLOCK * SC_ITEMS)) {
+    unsigned k[SC_ITEMS];
+    V v[SC_ITEMS];
 #pragma unroll
-  for (int u = 0; u < SC_ITEMS; u++) {
-    const long i = i0 + (long)u * RK_BLOCK;
-    k[u] = i < n ? __ldcs(idx + i) : 0u;
-  }
+    for (int u = 0; u < SC_ITEMS; u++) {
+      const long i = i0 + (long)u * RK_BLOCK;
+      k[u] = i < n ? __ldcs(idx + i) : 0u;
+    }
 #pragma unroll
-  for (int u = 0; u < SC_ITEMS; u++)
-    if (i0 + (long)u * RK_BLOCK < n) v[u] = __ldg(s + k[u]);
+    for (int u = 0; u < SC_ITEMS; u++)
+      if (i0 + (long)u * RK_BLOCK < n) v[u] = __ldg(s + k[u]);
 #pragma unroll
-  for (int u = 0; u < SC_ITEMS; u++) {
-    const long i = i0 + (long)u * RK_BLOCK;
-    if (i < n) __stcs(d + i, v[u]);
+    for (int u = 0; u < SC_ITEMS; u++) {
+      const long i = i0 + (long)u * RK_BLOCK;
+      if (i < n) __stcs(d + i, v[u]);
+    }
   }
 }
 
@@ -776,15 +753,24 @@ inline size_t rk_state_bytes(long n) { return (size_t)rk_tiles(n) * 256 * 4; }
 // top-8-bit windows of [0, n)
 inline int window_shift(int n) { int b = bit_length((unsigned)(n > 1 ? n - 1 : 1)); return b > 8 ? b - 8 : 0; }
 
+// the window counts of every tile of idx[0, n) and the gate word
+inline void ws_hist(const int *idx, long n, int shift, int wbits, int tiles, unsigned *counts, unsigned *unsorted) {
+  if (((uintptr_t)idx & 15) == 0)
+    k_ws_hist<true><<<tiles, RK_BLOCK, 0, stream()>>>((const unsigned *)idx, n, shift, wbits, counts, unsorted);
+  else
+    k_ws_hist<false><<<tiles, RK_BLOCK, 0, stream()>>>((const unsigned *)idx, n, shift, wbits, counts, unsorted);
+  launch_check("k_ws_hist");
+}
+
 // ------------------------------------------------ partitioned scatter ---
 // d[idx[k]] = s[k] for k < n (idx in [0, n_d)) when d is larger than L2 can
 // absorb random writes to (each would cost a DRAM read-modify-write of a
 // sector): the (index, value) pairs are split by destination window (windows
-// of about 32 MB, at most 256, with the same histogram, scan and split passes
-// as the partitioned gather), then written window by window while each window
-// sits in L2.  Ascending indices take one streaming scatter instead; the
+// of at most 8 MB, at most 256 of them, with the same histogram, scan and
+// split passes as the partitioned gather), then written window by window
+// while each window sits in L2.  Ascending indices take one streaming scatter instead; the
 // device decides (the kernels of the branch not taken return at once).
-struct ScatterLayout { size_t kout, vout, counts, totals, flags, total; };
+struct ScatterLayout { size_t kout, vout, counts, scan, flags, total; };
 inline ScatterLayout scatter_layout(long n, size_t vsize) {
   ScatterLayout L;
   size_t o = 0;
@@ -792,18 +778,31 @@ inline ScatterLayout scatter_layout(long n, size_t vsize) {
   L.kout = take((size_t)n * 4);
   L.vout = take((size_t)n * vsize);
   L.counts = take((size_t)rk_tiles(n) * WS_MAXW * 4);
-  L.totals = take(WS_MAXW * 4);
+  L.scan = take((size_t)add_suz_scratch(rk_tiles(n) * WS_MAXW) * 8);
   L.flags = take(256);
   L.total = o + 256;  // room to align the base
   return L;
 }
 bool scatter_partitioned_wanted(long n_d, size_t vsize) { return (size_t)n_d * vsize > (size_t)RK_DIRECT_MAX * 4; }
 size_t scatter_partitioned_bytes(long n, size_t vsize) { return scatter_layout(n, vsize).total; }
-// windows of about 32 MB of `bytes`, a power of two from 2 to 256: (log2 of
-// the count, shift of an index of [0, len) to its window)
-inline void ws_windows(size_t bytes, long len, int *wbits, int *shift) {
-  int wb = 1;
-  while (wb < 8 && (bytes >> wb) > ((size_t)32 << 20)) ++wb;
+// Window sizes, measured on int32 permutations: the gather runs fastest
+// with at least 8 windows of at most 64 MB (2.81 -> 2.69 ms at 2^28 against
+// 32 MB windows), the scatter with windows of at most 8 MB (2^28: 3.28 ms
+// with 32 MB windows, 3.06 with 16, 2.78 with 8; 2^25: 0.45, 0.40, 0.36).
+#ifndef GCVL_WS_GATHER_MB
+#define GCVL_WS_GATHER_MB 64
+#endif
+#ifndef GCVL_WS_GATHER_MINBITS
+#define GCVL_WS_GATHER_MINBITS 3
+#endif
+#ifndef GCVL_WS_SCATTER_MB
+#define GCVL_WS_SCATTER_MB 8
+#endif
+// windows of at most `mb` MB of `bytes`, a power of two from 2^min_bits to
+// 256: (log2 of the count, shift of an index of [0, len) to its window)
+inline void ws_windows(size_t bytes, long len, int mb, int min_bits, int *wbits, int *shift) {
+  int wb = min_bits;
+  while (wb < 8 && (bytes >> wb) > ((size_t)mb << 20)) ++wb;
   const int nb = bit_length((unsigned)(len > 1 ? len - 1 : 1));
   *wbits = wb;
   *shift = nb > wb ? nb - wb : 0;
@@ -820,10 +819,10 @@ void scatter_partitioned(V *d, const V *s, const int *idx, int n, int n_d, vec_p
   unsigned *kout = (unsigned *)(mem + L.kout);
   V *vout = (V *)(mem + L.vout);
   unsigned *counts = (unsigned *)(mem + L.counts);
-  unsigned *totals = (unsigned *)(mem + L.totals);
+  void *scan_scratch = mem + L.scan;
   unsigned *unsorted = (unsigned *)(mem + L.flags);  // the gate: non-zero when some index exceeds its successor
   int wbits, shift;
-  ws_windows((size_t)n_d * sizeof(V), n_d, &wbits, &shift);
+  ws_windows((size_t)n_d * sizeof(V), n_d, GCVL_WS_SCATTER_MB, 1, &wbits, &shift);
   const int nw = 1 << wbits;
   const int tiles = rk_tiles(n);
   constexpr size_t smem = ws_split_smem<V, true>();
@@ -834,15 +833,11 @@ void scatter_partitioned(V *d, const V *s, const int *idx, int n, int n_d, vec_p
     attr = true;
   }
   if (!GCVL_CK(cudaMemsetAsync(unsorted, 0, 4, S.stream))) return;
-  k_ws_hist<<<tiles, RK_BLOCK, 0, S.stream>>>((const unsigned *)idx, n, shift, nw, counts, unsorted);
-  launch_check("k_ws_hist");
+  ws_hist(idx, n, shift, wbits, tiles, counts, unsorted);
   k_sorted_scatter<V><<<sc_grid(n), RK_BLOCK, 0, S.stream>>>(d, s, idx, n, unsorted);
   launch_check("k_sorted_scatter");
-  k_ws_totals<<<nw, RK_BLOCK, 0, S.stream>>>(counts, tiles, totals, unsorted);
-  launch_check("k_ws_totals");
-  k_ws_scan<<<nw, WS_SCAN, 0, S.stream>>>(counts, tiles, nw, totals, unsorted);
-  launch_check("k_ws_scan");
-  k_window_split<false, V, true><<<tiles, RK_BLOCK, smem, S.stream>>>((const unsigned *)idx, n, shift, nw, counts,
+  add_suz(counts, counts, nw * tiles, scan_scratch);  // first slot of every (window, tile)
+  k_window_split<false, V, true><<<tiles, RK_BLOCK, smem, S.stream>>>((const unsigned *)idx, n, shift, wbits, counts,
                                                                       unsorted, kout, nullptr, s, vout);
   launch_check("k_window_split");
   k_window_scatter<V><<<sc_blocks(n), RK_BLOCK, 0, S.stream>>>(d, kout, vout, n, unsorted);
@@ -853,14 +848,14 @@ void scatter_partitioned(V *d, const V *s, const int *idx, int n, int n_d, vec_p
 // d[k] = s[idx[k]] for k < n (idx in [0, n_src)) when s is larger than L2 can
 // serve random reads from: each random 4- or 8-byte read from DRAM costs a
 // whole sector, and most miss.  Instead the indices are split by source
-// window (windows of about 32 MB, at most 256 of them), with pos[k] = where
+// window (at least 8 windows of at most 64 MB, at most 256), with pos[k] = where
 // index k went; a gather in window order reads each window of s while it
 // sits in L2, into p; and d[k] = p[pos[k]] reads p through as many sequential
 // runs as there are windows, few enough that L1 and L2 keep each run's
 // current lines.  The passes stream: 4 (histogram) + 12 (split) + 12 + 12
 // bytes per 4-byte element.  Ascending indices take one plain gather
 // instead; the device decides, as for the scatter.
-struct GatherLayout { size_t kout, pos, p, counts, totals, flags, total; };
+struct GatherLayout { size_t kout, pos, p, counts, scan, flags, total; };
 inline GatherLayout gather_layout(long n, size_t vsize) {
   GatherLayout L;
   size_t o = 0;
@@ -869,7 +864,7 @@ inline GatherLayout gather_layout(long n, size_t vsize) {
   L.pos = take((size_t)n * 4);
   L.p = vsize == 4 ? L.kout : take((size_t)n * vsize);  // 4-byte values overwrite their keys in place
   L.counts = take((size_t)rk_tiles(n) * WS_MAXW * 4);
-  L.totals = take(WS_MAXW * 4);
+  L.scan = take((size_t)add_suz_scratch(rk_tiles(n) * WS_MAXW) * 8);
   L.flags = take(256);
   L.total = o + 256;  // room to align the base
   return L;
@@ -891,23 +886,19 @@ void gather_partitioned(V *d, const V *s, const int *idx, int n, int n_src, vec_
   unsigned *pos = (unsigned *)(mem + L.pos);
   V *p = (V *)(mem + L.p);
   unsigned *counts = (unsigned *)(mem + L.counts);
-  unsigned *totals = (unsigned *)(mem + L.totals);
+  void *scan_scratch = mem + L.scan;
   unsigned *unsorted = (unsigned *)(mem + L.flags);  // the gate: non-zero when some index exceeds its successor
   int wbits, shift;
-  ws_windows((size_t)n_src * sizeof(V), n_src, &wbits, &shift);
+  ws_windows((size_t)n_src * sizeof(V), n_src, GCVL_WS_GATHER_MB, GCVL_WS_GATHER_MINBITS, &wbits, &shift);
   const int nw = 1 << wbits;
   const int tiles = rk_tiles(n);
   GCVL_CK(cudaMemsetAsync(unsorted, 0, 4, S.stream));
-  k_ws_hist<<<tiles, RK_BLOCK, 0, S.stream>>>((const unsigned *)idx, n, shift, nw, counts, unsorted);
-  launch_check("k_ws_hist");
-  k_gather_gated<V><<<sc_blocks(n), RK_BLOCK, 0, S.stream>>>(d, s, (const unsigned *)idx, n, unsorted, 0);
+  ws_hist(idx, n, shift, wbits, tiles, counts, unsorted);
+  k_gather_gated<V><<<sc_grid(n), RK_BLOCK, 0, S.stream>>>(d, s, (const unsigned *)idx, n, unsorted, 0);
   launch_check("k_gather_gated");
-  k_ws_totals<<<nw, RK_BLOCK, 0, S.stream>>>(counts, tiles, totals, unsorted);
-  launch_check("k_ws_totals");
-  k_ws_scan<<<nw, WS_SCAN, 0, S.stream>>>(counts, tiles, nw, totals, unsorted);
-  launch_check("k_ws_scan");
+  add_suz(counts, counts, nw * tiles, scan_scratch);  // first slot of every (window, tile)
   k_window_split<true><<<tiles, RK_BLOCK, ws_split_smem<unsigned, false>(), S.stream>>>(
-      (const unsigned *)idx, n, shift, nw, counts, unsorted, kout, pos);
+      (const unsigned *)idx, n, shift, wbits, counts, unsorted, kout, pos);
   launch_check("k_window_split");
   k_window_gather<V><<<sc_blocks(n), RK_BLOCK, 0, S.stream>>>(p, s, kout, n, (unsigned)n_src, unsorted,
                                                               S.d_status);

@@ -238,3 +238,23 @@ def test_segmented_default_permute_last_writer_wins(gpu, oracle):
     flags = (r.random(n) < 0.5).astype(np.int32)
     compare("exact", ops.fpm_e(gpu, "fpm_pez", x, idx, flags, lens, lens),
             ops.fpm_e(oracle, "fpm_pez", x, idx, flags, lens, lens))
+
+
+@pytest.mark.parametrize("kind", ["perm", "dups"])
+def test_partitioned_paths_unaligned_indices(gpu, oracle, kind):
+    """Index vectors 8 bytes off a 16-byte boundary: the window histogram
+    reads them one key at a time instead of four (gather and scatter)."""
+    from neslgpu_gb300.cvl import load
+    from neslgpu_gb300.ops import DeviceRunner
+    R = DeviceRunner(load(), offset=1)
+    c = R.cvl
+    r = W.rng(808)
+    x = r.integers(-(2 ** 31), 2 ** 31, size=NG, dtype=np.int64).astype(np.int32)
+    idx = (r.permutation(NG) if kind == "perm" else r.integers(0, NG, size=NG)).astype(np.int32)
+    a, ix, d = R.vec(x, "z"), R.vec(idx, "z"), R.out(NG, "z")
+    c.bck_puz(d.ptr, a.ptr, ix.ptr, NG, NG, None)
+    compare("exact", R.get(d, NG), ops.bck_u(oracle, "bck_puz", x, idx))
+    if kind == "perm":
+        c.smp_puz(d.ptr, a.ptr, ix.ptr, NG, None)
+        compare("exact", R.get(d, NG), ops.smp_u(oracle, "smp_puz", x, idx))
+    R.done()
