@@ -45,8 +45,14 @@ constexpr int RK_MAXPASS = 12;
 #ifndef GCVL_RK_LB
 #define GCVL_RK_LB 4
 #endif
+// Resident CTAs per SM the register allocation must allow: 32-bit keys
+// without segment numbers fit 64 registers (the pass holds its keys and
+// values in registers); 64-bit keys and segmented passes would spill there.
 #ifndef GCVL_RK_MINB
 #define GCVL_RK_MINB 2
+#endif
+#ifndef GCVL_RK_MINB_NARROW
+#define GCVL_RK_MINB_NARROW 4
 #endif
 constexpr int RK_LB = GCVL_RK_LB;  // predecessors read per look-back round trip
 constexpr int RK_DIRECT_MAX = 1 << 23;
@@ -217,8 +223,7 @@ template <class K, class V> struct PassArgs {
 };
 
 template <class K, class V, bool AUX, bool STABLE = true> constexpr size_t pass_smem() {
-  return (size_t)RK_TILE * (2 * sizeof(K) + 2 * sizeof(V) + (AUX ? 8 : 0)) + RK_WARPS * 256 * 2 + 256 * 4 +
-         256 * 8;
+  return (size_t)RK_TILE * (sizeof(K) + sizeof(V) + (AUX ? 4 : 0)) + RK_WARPS * 256 * 2 + 256 * 4 + 256 * 8;
 }
 
 // Publish this tile's count of one bin (digit or window), then look back for
@@ -269,18 +274,19 @@ __device__ __forceinline__ unsigned bin_lookback(unsigned *state, int tile, int 
 // STABLE: equal digits keep their order (every pass of a rank).  A pass
 // that only groups pairs by output window (the partitioned scatter) need
 // not: its slots come from shared-memory atomics instead of ballots.
+template <class K, bool AUX> constexpr int rk_minb() { return sizeof(K) == 4 && !AUX ? GCVL_RK_MINB_NARROW : GCVL_RK_MINB; }
 template <class K, class V, bool AUX, int IN, int OUT, bool STABLE = true>
-__global__ void __launch_bounds__(RK_BLOCK, GCVL_RK_MINB) k_radix_pass(PassArgs<K, V> a) {
+__global__ void __launch_bounds__(RK_BLOCK, rk_minb<K, AUX>()) k_radix_pass(PassArgs<K, V> a) {
   typedef unsigned short CntT;  // per-warp digit counts (at most 512)
+  // 32-bit keys and values leave the reorder as one 8-byte pair
+  constexpr bool PAIR = sizeof(K) == 4 && sizeof(V) == 4 && OUT == OUT_ARRAYS;
   extern __shared__ __align__(16) unsigned char rk_smem[];
-  // staged tile (input order) and the reordered tile
+  // the reordered tile (the input stays in registers)
   long long *s_gb = (long long *)rk_smem;                  // [256] global base per digit
-  K *s_kin = (K *)(s_gb + 256);
-  K *s_kout = s_kin + RK_TILE;
-  V *s_vin = (V *)(s_kout + RK_TILE);
-  V *s_vout = s_vin + RK_TILE;
-  unsigned *s_ain = (unsigned *)(s_vout + RK_TILE);
-  unsigned *s_aout = s_ain + (AUX ? RK_TILE : 0);
+  K *s_kout = (K *)(s_gb + 256);
+  V *s_vout = (V *)(s_kout + RK_TILE);
+  uint2 *s_pair = (uint2 *)s_kout;                         // PAIR: [RK_TILE] (key, value)
+  unsigned *s_aout = (unsigned *)(s_vout + RK_TILE);
   unsigned *s_loc = s_aout + (AUX ? RK_TILE : 0);          // [256] tile offset per digit
   CntT *s_cnt = (CntT *)(s_loc + 256);                      // [RK_WARPS][256]
   __shared__ unsigned s_tile;
@@ -295,35 +301,41 @@ __global__ void __launch_bounds__(RK_BLOCK, GCVL_RK_MINB) k_radix_pass(PassArgs<
   const long base = (long)tile * RK_TILE;
   const int valid = (int)min((long)RK_TILE, (long)a.n - base);
 
-  // stage the tile: every load of the thread in flight at once
+  // each warp's 32 * RK_ITEMS consecutive elements straight into registers
+  // (element wbase + 32c + lane in item c: coalesced, every load in flight)
+  const int wbase = warp * 32 * RK_ITEMS;
+  K kr[RK_ITEMS];
+  V vr[RK_ITEMS];
+  unsigned ar[AUX ? RK_ITEMS : 1];
 #pragma unroll
   for (int c = 0; c < RK_ITEMS; c++) {
-    const int e = c * RK_BLOCK + tid;
+    const int e = wbase + c * 32 + lane;
+    kr[c] = 0;
+    vr[c] = 0;
+    if (AUX) ar[c] = 0;
     if (e < valid) {
       if constexpr (IN == IN_SRC) {
         if constexpr (sizeof(K) == 8)
-          s_kin[e] = (K)rk_key64(__ldcs((const unsigned long long *)a.src + base + e), a.up);
+          kr[c] = (K)rk_key64(__ldcs((const unsigned long long *)a.src + base + e), a.up);
         else
-          s_kin[e] = (K)rk_key32(__ldcs((const unsigned *)a.src + base + e), a.up);
-        s_vin[e] = (V)(base + e);
+          kr[c] = (K)rk_key32(__ldcs((const unsigned *)a.src + base + e), a.up);
+        vr[c] = (V)(base + e);
       } else {
-        s_kin[e] = __ldcs(a.kin + base + e);
-        s_vin[e] = __ldcs(a.vin + base + e);
-        if (AUX) s_ain[e] = __ldcs(a.ain + base + e);
+        kr[c] = __ldcs(a.kin + base + e);
+        vr[c] = __ldcs(a.vin + base + e);
+        if (AUX) ar[c] = __ldcs(a.ain + base + e);
       }
     }
   }
-  __syncthreads();
 
   // rank within each warp's 512 elements: (rank << 8) | digit
-  const int wbase = warp * 32 * RK_ITEMS;
   CntT *cnt = s_cnt + warp * 256;
   const unsigned lt = (1u << lane) - 1u;
   unsigned wr[RK_ITEMS];
 #pragma unroll
   for (int c = 0; c < RK_ITEMS; c++) {
     const int e = wbase + c * 32 + lane;
-    const int d = e < valid ? (int)((s_kin[e] >> a.shift) & 255) : -1;
+    const int d = e < valid ? (int)((kr[c] >> a.shift) & 255) : -1;
     unsigned r = 0;
     if constexpr (STABLE) {
       const unsigned peers = warp_match8(d);
@@ -389,9 +401,8 @@ __global__ void __launch_bounds__(RK_BLOCK, GCVL_RK_MINB) k_radix_pass(PassArgs<
       pos[c] = 0;
       if (x != 0xFFFFFFFFu) {
         const int d = (int)(x & 255u);
-        const int e = wbase + c * 32 + lane;
         long long g = s_gb[d] + s_cnt[warp * 256 + d] + (x >> 8);
-        if (a.segoff) g -= __ldg(a.segoff + (int)s_kin[e]);
+        if (a.segoff) g -= __ldg(a.segoff + (int)kr[c]);
         pos[c] = (unsigned)g;
       }
     }
@@ -401,9 +412,8 @@ __global__ void __launch_bounds__(RK_BLOCK, GCVL_RK_MINB) k_radix_pass(PassArgs<
     __syncthreads();
 #pragma unroll
     for (int c = 0; c < RK_ITEMS; c++) {
-      const int e = wbase + c * 32 + lane;
       if (wr[c] != 0xFFFFFFFFu) {
-        const unsigned w = (unsigned)s_vin[e] >> a.wshift;
+        const unsigned w = (unsigned)vr[c] >> a.wshift;
         wr[c] = (atomicAdd(s_wc + w, 1u) << 8) | w;
       }
     }
@@ -432,9 +442,8 @@ __global__ void __launch_bounds__(RK_BLOCK, GCVL_RK_MINB) k_radix_pass(PassArgs<
     for (int c = 0; c < RK_ITEMS; c++) {
       const unsigned x = wr[c];
       if (x != 0xFFFFFFFFu) {
-        const int e = wbase + c * 32 + lane;
         const unsigned lp = s_loc[x & 255u] + (x >> 8);
-        s_ov[lp] = (unsigned)s_vin[e];
+        s_ov[lp] = (unsigned)vr[c];
         s_vout[lp] = (V)pos[c];
       }
     }
@@ -455,27 +464,39 @@ __global__ void __launch_bounds__(RK_BLOCK, GCVL_RK_MINB) k_radix_pass(PassArgs<
     if (x != 0xFFFFFFFFu) {
       const int d = (int)(x & 255u);
       const unsigned lp = s_cnt[warp * 256 + d] + (x >> 8);
-      const int e = wbase + c * 32 + lane;
-      s_kout[lp] = s_kin[e];
-      s_vout[lp] = s_vin[e];
-      if (AUX) s_aout[lp] = s_ain[e];
+      if constexpr (PAIR) {
+        s_pair[lp] = make_uint2((unsigned)kr[c], (unsigned)vr[c]);
+      } else {
+        s_kout[lp] = kr[c];
+        s_vout[lp] = vr[c];
+      }
+      if (AUX) s_aout[lp] = ar[c];
     }
   }
   __syncthreads();
   // coalesced runs out
 #pragma unroll 4
   for (int e = tid; e < valid; e += RK_BLOCK) {
-    const K k = s_kout[e];
+    K k;
+    V vv;
+    if constexpr (PAIR) {
+      const uint2 kv = s_pair[e];
+      k = (K)kv.x;
+      vv = (V)kv.y;
+    } else {
+      k = s_kout[e];
+      vv = s_vout[e];
+    }
     const int d = (int)((k >> a.shift) & 255);
     const long g = s_gb[d] + e;
     if (OUT == OUT_ARRAYS) {
       a.kout[g] = k;
-      a.vout[g] = s_vout[e];
+      a.vout[g] = vv;
       if (AUX) a.aout[g] = s_aout[e];
     } else {  // OUT_RANK
       int r = (int)g;
       if (a.segoff) r -= __ldg(a.segoff + (int)k);
-      a.rank[(unsigned)s_vout[e]] = r;
+      a.rank[(unsigned)vv] = r;
     }
   }
 }
