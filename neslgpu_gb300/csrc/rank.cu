@@ -13,11 +13,12 @@
 // GPU design (onesweep style).  One prepare pass builds every pass's 256-bin
 // digit histogram at once with shared-memory atomics (and, for segmented
 // ranks, writes transformed keys, indices and segment numbers).  Then one
-// pass per 8-bit digit: a CTA stages its 4096-element tile in shared memory,
-// ranks it stably per warp with ballots, learns how many earlier tiles'
-// elements fall in each digit by a per-digit decoupled look-back, reorders
-// the tile in shared memory and writes coalesced runs.  The first pass of an
-// unsegmented rank reads the caller's keys and transforms them itself.
+// pass per 8-bit digit: each warp of a CTA loads its 32 x RK_ITEMS
+// consecutive keys and values into registers, ranks them stably with
+// ballots, the CTA learns how many earlier tiles' elements fall in each
+// digit by a per-digit decoupled look-back, reorders the tile in shared
+// memory and writes coalesced runs.  The first pass of an unsegmented rank
+// reads the caller's keys and transforms them itself.
 //
 // The result is the inverse of the sort permutation: rank[index] = position,
 // a scatter to random places.  Below RK_DIRECT_MAX elements the last pass
@@ -27,8 +28,9 @@
 // element's slot from a second per-window look-back in the same pass -- and
 // a streaming kernel writes each window's ranks while the window sits in
 // L2, so DRAM sees whole sectors instead of a read-modify-write per 4-byte
-// element.  smp_pu* uses the same window partition (a pass of its own) and
-// window scatter for large vectors.
+// element.  Large permutes and gathers (smp_pu*, bck_pu*, the default and
+// flag permutes) split their pairs by window with passes of their own (the
+// window split below) and share the window scatter.
 #include "gcvl.cuh"
 
 #include <type_traits>
@@ -36,8 +38,12 @@
 
 namespace gcvl {
 
+// Keys per thread of a digit pass (tile = 256 x RK_ITEMS), and the CTAs per
+// SM of the 32-bit unsegmented passes, measured at 2^28 (int / double /
+// segmented int rank): 16 items at 4 CTAs 9.09 / 21.4 / 18.0 ms; 20 at 3
+// 9.06 / 19.8 / 17.2; 24 at 3 9.43 / 18.7 / 17.0; 32 at 2 10.1 / 25.9 / 21.9.
 #ifndef GCVL_RK_ITEMS
-#define GCVL_RK_ITEMS 16
+#define GCVL_RK_ITEMS 20
 #endif
 constexpr int RK_BLOCK = 256, RK_ITEMS = GCVL_RK_ITEMS, RK_TILE = RK_BLOCK * RK_ITEMS;
 constexpr int RK_WARPS = RK_BLOCK / 32;
@@ -52,7 +58,7 @@ constexpr int RK_MAXPASS = 12;
 #define GCVL_RK_MINB 2
 #endif
 #ifndef GCVL_RK_MINB_NARROW
-#define GCVL_RK_MINB_NARROW 4
+#define GCVL_RK_MINB_NARROW 3
 #endif
 constexpr int RK_LB = GCVL_RK_LB;  // predecessors read per look-back round trip
 constexpr int RK_DIRECT_MAX = 1 << 23;
@@ -277,7 +283,7 @@ __device__ __forceinline__ unsigned bin_lookback(unsigned *state, int tile, int 
 template <class K, bool AUX> constexpr int rk_minb() { return sizeof(K) == 4 && !AUX ? GCVL_RK_MINB_NARROW : GCVL_RK_MINB; }
 template <class K, class V, bool AUX, int IN, int OUT, bool STABLE = true>
 __global__ void __launch_bounds__(RK_BLOCK, rk_minb<K, AUX>()) k_radix_pass(PassArgs<K, V> a) {
-  typedef unsigned short CntT;  // per-warp digit counts (at most 512)
+  typedef unsigned short CntT;  // per-warp digit counts (at most 32 * RK_ITEMS)
   // 32-bit keys and values leave the reorder as one 8-byte pair
   constexpr bool PAIR = sizeof(K) == 4 && sizeof(V) == 4 && OUT == OUT_ARRAYS;
   extern __shared__ __align__(16) unsigned char rk_smem[];
@@ -437,23 +443,19 @@ __global__ void __launch_bounds__(RK_BLOCK, rk_minb<K, AUX>()) k_radix_pass(Pass
       s_gb[tid] = (long long)__ldg(a.wstarts + tid) + (long long)wprefix - (long long)wloc;
     }
     __syncthreads();
-    unsigned *s_ov = (unsigned *)s_kout;  // v by window slot
+    uint2 *s_vp = (uint2 *)s_kout;  // (v, position) by window slot: one 8-byte store
 #pragma unroll
     for (int c = 0; c < RK_ITEMS; c++) {
       const unsigned x = wr[c];
-      if (x != 0xFFFFFFFFu) {
-        const unsigned lp = s_loc[x & 255u] + (x >> 8);
-        s_ov[lp] = (unsigned)vr[c];
-        s_vout[lp] = (V)pos[c];
-      }
+      if (x != 0xFFFFFFFFu) s_vp[s_loc[x & 255u] + (x >> 8)] = make_uint2((unsigned)vr[c], pos[c]);
     }
     __syncthreads();
 #pragma unroll 4
     for (int e = tid; e < valid; e += RK_BLOCK) {
-      const unsigned v = s_ov[e];
-      const long g = s_gb[v >> a.wshift] + e;
-      a.pidx[g] = v;
-      a.ppos[g] = (unsigned)s_vout[e];
+      const uint2 vp = s_vp[e];
+      const long g = s_gb[vp.x >> a.wshift] + e;
+      a.pidx[g] = vp.x;
+      a.ppos[g] = vp.y;
     }
     return;
   }
@@ -771,6 +773,7 @@ inline int sc_grid(long n) {
   return (int)(need < cap ? (need < 1 ? 1 : need) : cap);
 }
 inline size_t rk_state_bytes(long n) { return (size_t)rk_tiles(n) * 256 * 4; }
+inline int ws_tiles(long n) { return (int)((n + WS_TILE - 1) / WS_TILE); }  // tiles of the window split
 // top-8-bit windows of [0, n)
 inline int window_shift(int n) { int b = bit_length((unsigned)(n > 1 ? n - 1 : 1)); return b > 8 ? b - 8 : 0; }
 
@@ -798,8 +801,8 @@ inline ScatterLayout scatter_layout(long n, size_t vsize) {
   auto take = [&](size_t bytes) { size_t at = o; o += align_up(bytes, 256); return at; };
   L.kout = take((size_t)n * 4);
   L.vout = take((size_t)n * vsize);
-  L.counts = take((size_t)rk_tiles(n) * WS_MAXW * 4);
-  L.scan = take((size_t)add_suz_scratch(rk_tiles(n) * WS_MAXW) * 8);
+  L.counts = take((size_t)ws_tiles(n) * WS_MAXW * 4);
+  L.scan = take((size_t)add_suz_scratch(ws_tiles(n) * WS_MAXW) * 8);
   L.flags = take(256);
   L.total = o + 256;  // room to align the base
   return L;
@@ -845,7 +848,7 @@ void scatter_partitioned(V *d, const V *s, const int *idx, int n, int n_d, vec_p
   int wbits, shift;
   ws_windows((size_t)n_d * sizeof(V), n_d, GCVL_WS_SCATTER_MB, 1, &wbits, &shift);
   const int nw = 1 << wbits;
-  const int tiles = rk_tiles(n);
+  const int tiles = ws_tiles(n);
   constexpr size_t smem = ws_split_smem<V, true>();
   static bool attr = false;
   if (!attr) {
@@ -884,8 +887,8 @@ inline GatherLayout gather_layout(long n, size_t vsize) {
   L.kout = take((size_t)n * 4);
   L.pos = take((size_t)n * 4);
   L.p = vsize == 4 ? L.kout : take((size_t)n * vsize);  // 4-byte values overwrite their keys in place
-  L.counts = take((size_t)rk_tiles(n) * WS_MAXW * 4);
-  L.scan = take((size_t)add_suz_scratch(rk_tiles(n) * WS_MAXW) * 8);
+  L.counts = take((size_t)ws_tiles(n) * WS_MAXW * 4);
+  L.scan = take((size_t)add_suz_scratch(ws_tiles(n) * WS_MAXW) * 8);
   L.flags = take(256);
   L.total = o + 256;  // room to align the base
   return L;
@@ -912,7 +915,7 @@ void gather_partitioned(V *d, const V *s, const int *idx, int n, int n_src, vec_
   int wbits, shift;
   ws_windows((size_t)n_src * sizeof(V), n_src, GCVL_WS_GATHER_MB, GCVL_WS_GATHER_MINBITS, &wbits, &shift);
   const int nw = 1 << wbits;
-  const int tiles = rk_tiles(n);
+  const int tiles = ws_tiles(n);
   GCVL_CK(cudaMemsetAsync(unsorted, 0, 4, S.stream));
   ws_hist(idx, n, shift, wbits, tiles, counts, unsorted);
   k_gather_gated<V><<<sc_grid(n), RK_BLOCK, 0, S.stream>>>(d, s, (const unsigned *)idx, n, unsorted, 0);

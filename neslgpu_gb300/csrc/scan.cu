@@ -297,6 +297,8 @@ template <class T> struct TArgs {
   int spin_limit;
   int *lead;  // reductions: per tile, the segment whose result lacks the earlier tiles' part (-1: none)
   int wmax;   // reductions: entries of the shared-memory offsets window
+  const int *gidx;  // gather-multiply form: element k is in[k] * gsrc[gidx[k]]
+  const T *gsrc;
 };
 
 // Segment offsets seen through the shared-memory window when possible.
@@ -417,8 +419,14 @@ template <int MODE> constexpr int cta_threads() { return MODE == M_REDUCE ? TT :
 #ifndef GCVL_RED_MINB_Z
 #define GCVL_RED_MINB_Z 8
 #endif
-template <class Op, int MODE, bool SEG, bool CHAIN = false>
-__global__ void __launch_bounds__(cta_threads<MODE>(), MODE == M_REDUCE ? (sizeof(typename Op::T) == 8 ? GCVL_RED_MINB_D : GCVL_RED_MINB_Z) : GCVL_SCAN_MINB) k_scan_tma(const __grid_constant__ CUtensorMap tin,
+// The gather-multiply form (a CSR sparse matrix-vector product: values by
+// TMA, column indices and the gathered vector entries by plain loads) holds
+// 16 more loads per thread in flight and runs 4 CTAs per SM.
+template <int MODE, class T, bool GATHER> constexpr int tma_minb() {
+  return GATHER ? 4 : MODE == M_REDUCE ? (sizeof(T) == 8 ? GCVL_RED_MINB_D : GCVL_RED_MINB_Z) : GCVL_SCAN_MINB;
+}
+template <class Op, int MODE, bool SEG, bool CHAIN = false, bool GATHER = false>
+__global__ void __launch_bounds__(cta_threads<MODE>(), tma_minb<MODE, typename Op::T, GATHER>()) k_scan_tma(const __grid_constant__ CUtensorMap tin,
                                                      const __grid_constant__ CUtensorMap tout,
                                                      TArgs<typename Op::T> a) {
   typedef typename Op::T T;
@@ -524,6 +532,27 @@ __global__ void __launch_bounds__(cta_threads<MODE>(), MODE == M_REDUCE ? (sizeo
   if constexpr (std::is_same<Op, CountB>::value) {
 #pragma unroll
     for (int i = 0; i < ITEMS; i++) x[i] = x[i] != 0;  // pk1_lev counts true flags
+  }
+  if constexpr (GATHER) {
+    // the products a BPERMUTE and an elementwise * would have materialised;
+    // gidx is 16-byte aligned and k0 a multiple of ITEMS, so a full row's
+    // indices are ITEMS/4 aligned 16-byte loads
+    int g[ITEMS];
+    if (cnt == ITEMS) {
+#pragma unroll
+      for (int c = 0; c < ITEMS / 4; c++) {
+        const int4 q = __ldcs(reinterpret_cast<const int4 *>(a.gidx + k0) + c);
+        g[4 * c] = q.x; g[4 * c + 1] = q.y; g[4 * c + 2] = q.z; g[4 * c + 3] = q.w;
+      }
+    } else {
+#pragma unroll
+      for (int i = 0; i < ITEMS; i++) g[i] = i < cnt ? __ldcs(a.gidx + k0 + i) : 0;
+    }
+    T v[ITEMS];
+#pragma unroll
+    for (int i = 0; i < ITEMS; i++) v[i] = i < cnt ? __ldg(a.gsrc + g[i]) : (T)0;
+#pragma unroll
+    for (int i = 0; i < ITEMS; i++) x[i] = i < cnt ? x[i] * v[i] : Op::ident();
   }
   // segment holding k0 (reductions): the last window entry <= k0
   int s0 = 0;
@@ -1421,6 +1450,35 @@ static void run_gather_mul_reduce(double *y, const double *vals, const int *cols
     GCVL_CK(cudaMemsetAsync(y, 0, (size_t)rows * sizeof(double), S.stream));
     return;
   }
+  const long trows = (long)nnz / row_items<double>();
+  CUtensorMap tin;
+  if (trows >= 1 && !((size_t)vals & 15) && !((size_t)cols & 15) && !getenv("GCVL_NO_TMA") &&
+      tma_map<double>(&tin, vals, trows)) {
+    // TMA tiles of the values, the fixed-point segmented fold of k_scan_tma
+    const int tiles = ceil_div(nnz, (long)TT * row_items<double>());
+    void *mem = scratch_or_work(scratch, reduce_pass_bytes(tiles));
+    if (!mem) return;
+    TArgs<double> t{};
+    t.out = y; t.in = vals; t.n = nnz; t.rows = trows;
+    t.sv = seg_view(sd, nnz, rows);
+    t.lb = lookback_carve(mem, tiles);
+    t.status = S.d_status;
+    t.spin_limit = S.spin_limit;
+    t.lead = (int *)((char *)t.lb.word + align_up((size_t)tiles * 16, 256));
+    t.wmax = wmax_for<double, M_REDUCE>(nnz, rows);
+    t.gidx = cols; t.gsrc = x;
+    GCVL_CK(cudaMemsetAsync(mem, 0, lookback_clear_bytes(tiles), S.stream));
+    GCVL_CK(cudaMemsetAsync(t.lead, 0xFF, (size_t)tiles * 4, S.stream));
+    if ((long)nnz < RED_CHAIN_MEAN * rows)
+      k_scan_tma<AddD, M_REDUCE, true, true, true>
+          <<<tiles, cta_threads<M_REDUCE>(), tma_smem<double>(t.wmax), S.stream>>>(tin, tin, t);
+    else
+      k_scan_tma<AddD, M_REDUCE, true, false, true>
+          <<<tiles, cta_threads<M_REDUCE>(), tma_smem<double>(t.wmax), S.stream>>>(tin, tin, t);
+    launch_check("gcvl_spmv_csr");
+    launch_tile_fix<AddD>(t.lb.word, t.lead, tiles, y);
+    return;
+  }
   const int tiles = ceil_div(nnz, tile_elems<double>());
   void *mem = scratch_or_work(scratch, reduce_pass_bytes(tiles));
   if (!mem) return;
@@ -1863,5 +1921,7 @@ GCVL_EXPORT void gcvl_spmv_csr(vec_p y, vec_p vals, vec_p cols, vec_p x, vec_p s
 }
 GCVL_EXPORT int gcvl_spmv_csr_scratch(int nnz, int rows) {
   (void)rows;
-  return (int)((reduce_pass_bytes(ceil_div(nnz > 0 ? nnz : 1, tile_elems<double>())) + 7) / 8);
+  const int k = nnz > 0 ? nnz : 1;  // either form's tiles
+  const int a = ceil_div(k, tile_elems<double>()), b = ceil_div(k, (long)TT * row_items<double>());
+  return (int)((reduce_pass_bytes(a > b ? a : b) + 7) / 8);
 }

@@ -116,22 +116,46 @@ def test_spmv_on_gpu(gpu, oracle):
     assert np.all(np.abs(got - want) <= 1e-12 * np.maximum(np.abs(want), S) + 1e-300)
 
 
+def _long_rows_csr(rows, ncols, seed):
+    """Rows of about 600 nonzeros: the unchained fold."""
+    r = np.random.default_rng(seed)
+    lens = r.integers(1, 1200, size=rows).astype(np.int32)
+    lens[r.random(rows) < 0.05] = 0
+    nnz = int(lens.sum())
+    return lens, r.integers(0, ncols, size=nnz).astype(np.int32), r.normal(size=nnz), r.normal(size=ncols)
+
+
 @pytest.mark.gpu
-def test_fused_spmv_matches_vcode_program(gpu, oracle):
+@pytest.mark.parametrize("case,offset", [("short", 0), ("short", 1), ("long", 0), ("many", 0)])
+def test_fused_spmv_matches_vcode_program(gpu, oracle, case, offset):
     """gcvl_spmv_csr (gather, multiply and per-row sum in one pass) against
-    the SPMV VCODE program on the oracle."""
-    from neslgpu_gb300.cvl import DeviceVector
-    c = gpu.cvl
-    lens, cols, vals, x = _csr(30_000, 7_000, 5)
-    want = _spmv(oracle.cvl, lens, cols, vals, x)
-    sd, nnz, rows = gpu.segd(lens)
-    cv, vv, xv = gpu.vec(cols, "z"), gpu.vec(vals, "d"), gpu.vec(x, "d")
-    y = gpu.out(rows, "d")
-    scr = gpu.units(c.gcvl_spmv_csr_scratch(nnz, rows))
+    the SPMV VCODE program on the oracle: power-law rows (the chained fold
+    for short rows), rows of about 600 nonzeros, vectors off a 16-byte
+    boundary (the form without TMA), and 2.8 million nonzeros (rows across
+    about 1,400 tiles)."""
+    from neslgpu_gb300.cvl import load
+    from neslgpu_gb300.ops import DeviceRunner
+    R = DeviceRunner(load(), offset=offset)
+    c = R.cvl
+    lens, cols, vals, x = {"short": lambda: _csr(30_000, 7_000, 5), "long": lambda: _long_rows_csr(3_000, 50_000, 6),
+                           "many": lambda: _csr(1_000_003, 1 << 21, 7)}[case]()
+    sd, nnz, rows = R.segd(lens)
+    cv, vv, xv = R.vec(cols, "z"), R.vec(vals, "d"), R.vec(x, "d")
+    y = R.out(rows, "d")
+    scr = R.units(c.gcvl_spmv_csr_scratch(nnz, rows))
     c.gcvl_spmv_csr(y.ptr, vv.ptr, cv.ptr, xv.ptr, sd.ptr, nnz, rows, scr.ptr)
-    got = gpu.get(y, rows)
-    gpu.done()
-    starts = np.cumsum(lens) - lens
-    S = np.array([np.abs(vals[s:s + l] * x[cols[s:s + l]]).sum() for s, l in zip(starts, lens)])
+    got = R.get(y, rows)
+    R.done()
+    nz = lens > 0
+    starts = (np.cumsum(lens, dtype=np.int64) - lens)[nz]
+    prod = vals * x[cols]
+
+    def row_sums(v):  # per row, empty rows 0
+        out = np.zeros(rows)
+        out[nz] = np.add.reduceat(v, starts)
+        return out
+    S = row_sums(np.abs(prod))
+    # the oracle's VCODE run at 2.8 million nonzeros takes too long: numpy row sums there
+    want = row_sums(prod) if case == "many" else _spmv(oracle.cvl, lens, cols, vals, x)
     assert np.all(np.abs(got - want) <= 1e-12 * np.maximum(np.abs(want), S) + 1e-300)
     assert np.all(got[lens == 0] == 0.0)
