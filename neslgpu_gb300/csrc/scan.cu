@@ -1316,6 +1316,7 @@ template <class Op, bool SEG, bool RED = false> int ring_grid(int tiles) {
 }
 
 // Returns false (nothing launched) when the vectors do not suit TMA.
+constexpr long RING_RED_MEAN = 32;
 template <class Op, int MODE, bool SEG>
 bool run_scan_tma(typename Op::T *out, const typename Op::T *in, vec_p sd, int n, int m, vec_p scratch,
                   const char *name) {
@@ -1346,9 +1347,14 @@ bool run_scan_tma(typename Op::T *out, const typename Op::T *in, vec_p sd, int n
   }
   if constexpr (MODE == M_REDUCE && SEG && !std::is_same<Op, AddD>::value) {
     // segmented reductions on the ring (results written at segment ends,
-    // the carry from the look-back: no fix-up pass)
+    // the carry from the look-back: no fix-up pass) when segments average
+    // RING_RED_MEAN elements or more.  Shorter ones stay on the tile kernel,
+    // whose offsets window finds each end's segment in shared memory: the
+    // ring looks every end up in global memory, and a quicksort's last
+    // levels (one- and few-element segments) ran 2x slower on it
+    // (0.42 -> 0.85 s for 2^26 keys).
     const int tiles = ceil_div(n, (long)RTT * row_items<T>());
-    const int grid = ring_grid<Op, SEG, true>(tiles);
+    const int grid = (long)n >= RING_RED_MEAN * m ? ring_grid<Op, SEG, true>(tiles) : 0;
     if (grid > 0) {
       if (!tma_map<T>(&tin, in, rows, RTT)) return false;
       void *mem = scratch_or_work(scratch, lookback_bytes(tiles));
