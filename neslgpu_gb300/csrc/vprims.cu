@@ -344,9 +344,55 @@ __device__ __forceinline__ bool lw_mark(unsigned *bits, long g) {  // true if g 
   const unsigned b = 1u << (g & 31);
   return (atomicOr(bits + (g >> 5), b) & b) != 0;
 }
-// destinations i[k] of the elements whose flag is set (all when f is null)
+// Destinations that strictly ascend cannot repeat: a streaming check sets
+// *need when they might (an index out of [0, n_d), or not above the one
+// before it), and only then does the bitmap pass run -- a quicksort's
+// DPERMUTEs ascend, and the bitmap's random atomics were most of their
+// cost.  One vote and at most one atomic per warp.
+__global__ void __launch_bounds__(VBLOCK) k_lw_ascent(const int *__restrict__ i, long n, long n_d, unsigned *need) {
+  bool bad = false;
+  const long stride = (long)gridDim.x * VBLOCK;
+  for (long k = (long)blockIdx.x * VBLOCK + threadIdx.x; k < n; k += stride) {
+    const int g = __ldg(i + k);
+    // the predecessor's load usually hits the line just read by the lane before
+    if (g < 0 || g >= n_d || (k > 0 && g <= __ldg(i + k - 1))) bad = true;
+  }
+  if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(need, 1u);
+}
+// The segmented form: within every source segment the local indices
+// strictly ascend and lie inside the matching destination segment (the
+// segments' destination ranges are disjoint and in order, so the global
+// destinations ascend too).
+__global__ void __launch_bounds__(VBLOCK) k_lw_ascent_seg(const int *__restrict__ i, SegView sv,
+                                                          const int *__restrict__ off_d, int m_d, unsigned *need) {
+  bool bad = false;
+  const long k0 = ((long)blockIdx.x * VBLOCK + threadIdx.x) * SITEMS;
+  if (k0 < sv.n) {
+    const int cnt = (int)min((long)SITEMS, (long)sv.n - k0);
+    int s = seg_of(sv, (int)k0);
+    int start = __ldg(sv.off + s), end = __ldg(sv.off + s + 1);
+    int len_d = s < m_d ? __ldg(off_d + s + 1) - __ldg(off_d + s) : 0;
+    int prev = (int)k0 > start ? __ldg(i + k0 - 1) : -1;
+    for (int q = 0; q < cnt; q++) {
+      const int k = (int)k0 + q;
+      while (k >= end) {
+        ++s; start = end; end = __ldg(sv.off + s + 1);
+        len_d = s < m_d ? __ldg(off_d + s + 1) - __ldg(off_d + s) : 0;
+        prev = -1;
+      }
+      const int g = __ldg(i + k);
+      if (s < m_d && (g < 0 || g >= len_d || g <= prev)) bad = true;
+      prev = g;
+    }
+  }
+  if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(need, 1u);
+}
+// destinations i[k] of the elements whose flag is set (all when f is null);
+// with `need`, only when *need is set
 __global__ void __launch_bounds__(VBLOCK) k_lw_detect(const int *__restrict__ i, const int *__restrict__ f, long n,
-                                                      long n_d, unsigned *bits, unsigned *flag) {
+                                                      long n_d, unsigned *bits, unsigned *flag,
+                                                      const unsigned *need) {
+  if (need && !lw_gate(need)) return;
   bool dup = false;
   const long stride = (long)gridDim.x * VBLOCK;
   for (long k = (long)blockIdx.x * VBLOCK + threadIdx.x; k < n; k += stride) {
@@ -417,16 +463,33 @@ inline int lw_grid(long n) {
   long g = (n + VBLOCK - 1) / VBLOCK, cap = (long)st().sm_count * 16;
   return (int)(g < 1 ? 1 : (g < cap ? g : cap));
 }
-// before the scatter: clear the bitmap and flag, mark the destinations
+// before the scatter: clear the bitmap and flags (flag[0]: some destination
+// repeats; flag[1]: the destinations may repeat), mark the destinations
+// unless they strictly ascend (forms without flags)
 inline void lw_detect(const LwMem &L, const int *i, const int *f, long n, long n_d) {
   GCVL_CK(cudaMemsetAsync(L.bits, 0, (size_t)(n_d + 31) / 32 * 4 + 16, stream()));
   if (n <= 0) return;
-  k_lw_detect<<<lw_grid(n), VBLOCK, 0, stream()>>>(i, f, n, n_d, L.bits, L.flag);
+  unsigned *need = nullptr;
+  if (!f) {
+    need = L.flag + 1;
+    k_lw_ascent<<<lw_grid(n), VBLOCK, 0, stream()>>>(i, n, n_d, need);
+    launch_check("k_lw_ascent");
+  }
+  k_lw_detect<<<lw_grid(n), VBLOCK, 0, stream()>>>(i, f, n, n_d, L.bits, L.flag, need);
   launch_check("k_lw_detect");
 }
 inline void lw_detect_seg(const LwMem &L, const int *i, const int *f, const SegView &ss, const SegView &sdd) {
   GCVL_CK(cudaMemsetAsync(L.bits, 0, (size_t)(sdd.n + 31) / 32 * 4 + 16, stream()));
-  segwalk(LwDetectSeg{i, f, sdd.off, sdd.m, (long)sdd.n, L.bits, L.flag}, ss, "k_lw_detect_seg");
+  const LwDetectSeg det{i, f, sdd.off, sdd.m, (long)sdd.n, L.bits, L.flag};
+  if (f || ss.n <= 0 || ss.m <= 0) {
+    segwalk(det, ss, "k_lw_detect_seg");
+    return;
+  }
+  const int grid = grid_for(((long)ss.n + SITEMS - 1) / SITEMS, VBLOCK);
+  k_lw_ascent_seg<<<grid, VBLOCK, 0, stream()>>>(i, ss, sdd.off, sdd.m, L.flag + 1);
+  launch_check("k_lw_ascent_seg");
+  k_segwalk_gated<<<grid, VBLOCK, 0, stream()>>>(det, ss, L.flag + 1);
+  launch_check("k_lw_detect_seg");
 }
 // after the scatter: the last writer of every destination, where some repeat
 template <class T> void lw_fix(T *d, const T *s, const LwMem &L, const int *i, const int *f, long n, long n_d) {

@@ -258,3 +258,24 @@ def test_partitioned_paths_unaligned_indices(gpu, oracle, kind):
         c.smp_puz(d.ptr, a.ptr, ix.ptr, NG, None)
         compare("exact", R.get(d, NG), ops.smp_u(oracle, "smp_puz", x, idx))
     R.done()
+
+
+@pytest.mark.parametrize("n", [5000, (1 << 23) + 4099])
+def test_default_permute_ascending_with_repeats(gpu, oracle, n):
+    """Sorted destinations with repeats are not strictly ascending: the
+    last-writer pass must still run (a strictly ascending index vector
+    skips it), unsegmented and segmented."""
+    r = W.rng(n + 1)
+    x = r.integers(-1000, 1000, size=n).astype(np.int32)
+    idx = np.sort(r.integers(0, n, size=n)).astype(np.int32)
+    dflt = np.full(n, -7, dtype=np.int32)
+    compare("exact", ops.dpe_u(gpu, "dpe_puz", x, idx, dflt), ops.dpe_u(oracle, "dpe_puz", x, idx, dflt))
+    lens = W.geometric_lengths(r, n, 40.0)
+    # local indices sorted within each segment, with repeats
+    loc = np.concatenate([np.sort(r.integers(0, L, size=L)) for L in lens]).astype(np.int32)
+    compare("exact", ops.dpe_e(gpu, "dpe_pez", x, loc, dflt, lens, lens),
+            ops.dpe_e(oracle, "dpe_pez", x, loc, dflt, lens, lens))
+    # strictly ascending within each segment: no repeats, the bitmap pass skipped
+    strict = np.concatenate([np.arange(L) for L in lens]).astype(np.int32)
+    compare("exact", ops.dpe_e(gpu, "dpe_pez", x, strict, dflt, lens, lens),
+            ops.dpe_e(oracle, "dpe_pez", x, strict, dflt, lens, lens))
