@@ -1316,7 +1316,10 @@ template <class Op, bool SEG, bool RED = false> int ring_grid(int tiles) {
 }
 
 // Returns false (nothing launched) when the vectors do not suit TMA.
-constexpr long RING_RED_MEAN = 32;
+#ifndef GCVL_RING_RED_MEAN
+#define GCVL_RING_RED_MEAN 32
+#endif
+constexpr long RING_RED_MEAN = GCVL_RING_RED_MEAN;
 template <class Op, int MODE, bool SEG>
 bool run_scan_tma(typename Op::T *out, const typename Op::T *in, vec_p sd, int n, int m, vec_p scratch,
                   const char *name) {
