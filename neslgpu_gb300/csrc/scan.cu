@@ -23,6 +23,7 @@
 #include "tma.cuh"
 
 #include <stdlib.h>
+#include <algorithm>
 #include <type_traits>
 
 namespace gcvl {
@@ -1158,6 +1159,223 @@ __global__ void __launch_bounds__(RTB, GCVL_RING_MINB)
   }
 }
 
+// ============================================================================
+// Segmented reductions of 4-byte elements along per-warp ranges.
+//
+// Each warp owns a contiguous range of chunks (32 rows of 32 elements, one
+// row per lane) and streams them through WR_NB chunk buffers of its own by
+// 2-D TMA copies (128B swizzle), so no warp waits for another and no CTA
+// barrier is taken.  Per chunk a lane folds its row, a warp segmented scan
+// gives each lane its prefix on top of the fold carried from the range's
+// earlier chunks, and one pass over the items records the running value at
+// every segment end in shared memory.  Then the lanes take the segments
+// whose last element lies in the chunk -- the next 32 offsets in one
+// coalesced load, as many rounds as needed -- and write each result (the
+// initial value for an empty segment).  Segment numbers come from the
+// offsets themselves, in order, instead of a search per end.  The one
+// result per range whose segment began in an earlier range holds only the
+// range's part; the range publishes (has a segment start, fold since its
+// last start) and k_tile_fix completes that result.
+// ============================================================================
+#ifndef GCVL_RED_WARP
+#define GCVL_RED_WARP 1
+#endif
+#ifndef GCVL_WR_NB
+#define GCVL_WR_NB 2
+#endif
+constexpr int WR_WARPS = 4, WR_NB = GCVL_WR_NB;
+constexpr int WR_ELEMS = 32 * 32;  // a chunk: a 32-element row per lane
+constexpr unsigned WR_CHUNK_BYTES = WR_ELEMS * 4;
+constexpr size_t wr_warp_bytes() { return (size_t)WR_NB * WR_CHUNK_BYTES; }
+constexpr size_t wr_smem() { return 1024 + WR_WARPS * wr_warp_bytes(); }
+
+template <class Op>
+__global__ void __launch_bounds__(WR_WARPS * 32)
+    k_segred_warp(const __grid_constant__ CUtensorMap tin, TArgs<typename Op::T> a, long chunks, int ranges) {
+  typedef typename Op::T T;
+  static_assert(sizeof(T) == 4, "rows of 32 four-byte elements");
+  extern __shared__ unsigned char dyn_smem[];
+  __shared__ unsigned long long s_bar[WR_WARPS][WR_NB];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int gw = blockIdx.x * WR_WARPS + warp;
+  if (gw >= ranges) return;  // a whole warp: nothing below meets other warps
+  unsigned char *buf = (unsigned char *)(((size_t)dyn_smem + 1023) & ~(size_t)1023) + (size_t)warp * wr_warp_bytes();
+  unsigned long long *bar = s_bar[warp];
+  const long c0 = (long)gw * chunks / ranges, c1 = (long)(gw + 1) * chunks / ranges;
+  const int nck = (int)(c1 - c0);
+  const long n = a.n;
+  const int m = a.sv.m;
+  if (lane == 0) {
+#pragma unroll
+    for (int j = 0; j < WR_NB; j++) mbar_init(&bar[j], 1);
+    fence_mbar_init();
+#pragma unroll
+    for (int j = 0; j < WR_NB; j++)
+      if (j < nck) {
+        mbar_arrive_expect_tx(&bar[j], WR_CHUNK_BYTES);
+        tma_load_2d(buf + j * WR_CHUNK_BYTES, &tin, &bar[j], 0, (int)((c0 + j) * 32));
+      }
+  }
+  __syncwarp();
+
+  int lim = a.spin_limit;  // after one timeout the remaining waits give up at once
+  // the next segment to finish: segments before it end at or before the range
+  int sp = gw == 0 ? 0 : seg_of(a.sv, (int)(c0 * WR_ELEMS));
+  T wc = Op::ident();  // fold of the open piece carried from the range's earlier chunks
+  bool wh = false;     // that piece starts at a segment start inside the range
+  int lead_l = -1;     // (lane) the result lacking the earlier ranges' part
+  // head-bit words of a row: this chunk's read a chunk ahead (the bitmap is
+  // streamed once, from DRAM); lane 31 also needs the next chunk's first
+  auto row_bits = [&](long cc) -> unsigned {
+    const long kk = cc * WR_ELEMS + lane * 32;
+    return cc < c1 && kk < n ? __ldg(a.sv.bits + (kk >> 5)) : 0u;
+  };
+  unsigned hw_next = row_bits(c0);
+  for (int ci = 0; ci < nck; ci++) {
+    const long c = c0 + ci;
+    const int b = ci % WR_NB;
+    const long cs = c * WR_ELEMS;
+    const long k0 = cs + lane * 32;
+    const int cnt = (int)max(0L, min(32L, n - k0));
+    // the chunk's independent loads go out before the wait for its rows: the
+    // next chunk's head bits, the first head bit after this chunk, the next
+    // 32 segment ends
+    const unsigned hw = hw_next;
+    hw_next = row_bits(c + 1);
+    unsigned nbw = 1u;
+    if (lane == 31 && cs + WR_ELEMS < n) nbw = __ldg(a.sv.bits + ((cs + WR_ELEMS) >> 5));
+    int o_next = sp + lane < m ? __ldg(a.sv.off + sp + lane + 1) : INT_MAX;
+    int po_first = lane == 0 && sp < m ? __ldg(a.sv.off + sp) : 0;
+    if (!mbar_wait(&bar[b], (unsigned)(ci / WR_NB) & 1u, lim)) {
+      atomicOr(a.status, DEV_TIMEOUT);
+      lim = 1;
+    }
+    T x[32];
+    if (c * 32 + lane < a.rows) {
+      const unsigned char *rowb = buf + b * WR_CHUNK_BYTES;
+#pragma unroll
+      for (int q = 0; q < 8; q++) {
+        const uint4 u = *(const uint4 *)(rowb + swz(lane, q));
+        memcpy(&x[4 * q], &u, 16);
+      }
+    } else {
+#pragma unroll
+      for (int i = 0; i < 32; i++) x[i] = i < cnt ? a.in[k0 + i] : Op::ident();
+    }
+    if constexpr (std::is_same<Op, CountB>::value) {
+#pragma unroll
+      for (int i = 0; i < 32; i++) x[i] = x[i] != 0;  // pk1_lev counts true flags
+    }
+    // the running value at each segment end, element p of the chunk at s_end[p]:
+    // the chunk's own buffer, each lane writing only the 128 bytes of the row
+    // it has just read (its own loads of them come first), the buffer refilled
+    // only once the chunk's results are out
+    T *s_end = (T *)(buf + b * WR_CHUNK_BYTES);
+    // head bits of the row; its last element ends a segment when the next
+    // element is a head or past the end
+    const unsigned heads = cnt >= 32 ? hw : (hw & ((1u << cnt) - 1u));
+    unsigned nb = __shfl_down_sync(0xffffffffu, hw & 1u, 1);
+    if (lane == 31) nb = nbw & 1u;
+    if (k0 + cnt >= n) nb = 1u;
+    const unsigned ends =
+        cnt == 0 ? 0u : (((heads >> 1) | (nb << (cnt - 1))) & (cnt >= 32 ? ~0u : ((1u << cnt) - 1u)));
+    // One pass over the row: the value at every segment end whose segment
+    // starts in the row is final and recorded at once; the row's first end,
+    // when its segment began before the row, waits for the lanes' prefix;
+    // what remains is the row's open piece (fold since its last head).
+    T r = Op::ident();
+    bool started = false;
+    T first_v = Op::ident();
+    int first_p = -1;
+    const int pbase = lane * 32;
+    if (cnt == 32) {
+#pragma unroll
+      for (int i = 0; i < 32; i++) {
+        if ((heads >> i) & 1u) { r = Op::apply(Op::init(), x[i]); started = true; }
+        else r = Op::apply(r, x[i]);
+        if ((ends >> i) & 1u) {
+          if (started) s_end[pbase + i] = r;
+          else { first_v = r; first_p = pbase + i; }
+        }
+      }
+    } else {
+#pragma unroll
+      for (int i = 0; i < 32; i++) {
+        if (i < cnt) {
+          if ((heads >> i) & 1u) { r = Op::apply(Op::init(), x[i]); started = true; }
+          else r = Op::apply(r, x[i]);
+          if ((ends >> i) & 1u) {
+            if (started) s_end[pbase + i] = r;
+            else { first_v = r; first_p = pbase + i; }
+          }
+        }
+      }
+    }
+    // the lanes' segmented scan of their open pieces, the value entering each row
+    int f = started;
+    T v = r;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const int f2 = shfl_up(f, d);
+      const T v2 = shfl_up(v, d);
+      if (lane >= d) { v = f ? v : Op::apply(v2, v); f |= f2; }
+    }
+    int ef = shfl_up(f, 1);
+    T ev = shfl_up(v, 1);
+    if (lane == 0) { ef = 0; ev = Op::ident(); }
+    if (first_p >= 0) {
+      s_end[first_p] = Op::apply(ef ? ev : Op::apply(wc, ev), first_v);
+      if (!ef && !wh) lead_l = -2 - first_p;  // marks the position; the segment is named below
+    }
+    const int lf = __shfl_sync(0xffffffffu, f, 31);
+    const T lv = __shfl_sync(0xffffffffu, v, 31);
+    if (lf) { wc = lv; wh = true; } else wc = Op::apply(wc, lv);
+    const unsigned ib = __ballot_sync(0xffffffffu, lead_l <= -2);
+    const int ipos = ib ? -2 - __shfl_sync(0xffffffffu, lead_l, __ffs(ib) - 1) : -1;
+    if (lead_l <= -2) lead_l = -1;
+    __syncwarp();  // the ends are recorded
+    // the segments whose last element lies in this chunk: off[s+1] in (cs, ce]
+    const long ce = min(cs + (long)WR_ELEMS, n);
+    for (int round = 0;; round++) {
+      const int sg = sp + lane;
+      const int o = round == 0 ? o_next : (sg < m ? __ldg(a.sv.off + sg + 1) : INT_MAX);
+      const bool fin = sg < m && (long)o <= ce;
+      const unsigned fb = __ballot_sync(0xffffffffu, fin);
+      int po = __shfl_up_sync(0xffffffffu, o, 1);
+      if (lane == 0) po = round == 0 ? po_first : (sp < m ? __ldg(a.sv.off + sp) : 0);
+      if (fin) {
+        if (po == o) {
+          a.out[sg] = Op::init();  // an empty segment
+        } else {
+          const int pe = (int)((long)o - 1 - cs);
+          a.out[sg] = s_end[pe];
+          if (pe == ipos) lead_l = sg;
+        }
+      }
+      const int k = __popc(fb);  // offsets ascend: the finished segments are a prefix of the lanes
+      sp += k;
+      if (k < 32) break;
+    }
+    __syncwarp();  // every read of the buffer is done
+    if (lane == 0 && ci + WR_NB < nck) {  // refill it
+      fence_proxy_async_smem();
+      mbar_arrive_expect_tx(&bar[b], WR_CHUNK_BYTES);
+      tma_load_2d(buf + b * WR_CHUNK_BYTES, &tin, &bar[b], 0, (int)((c + WR_NB) * 32));
+    }
+  }
+  const unsigned lb = __ballot_sync(0xffffffffu, lead_l >= 0);
+  const int lead = lb ? __shfl_sync(0xffffffffu, lead_l, __ffs(lb) - 1) : -1;
+  if (lane == 0) {
+    lb_publish(a.lb.word + gw, wh ? TS_INC : TS_AGG, to_bits<T>(wc));
+    if (lead >= 0) a.lead[gw] = lead;
+    // no copy may still be landing in the buffers when the warp leaves
+    for (int j = 0; j < WR_NB && j < nck; j++) {
+      const int last = j + WR_NB * ((nck - 1 - j) / WR_NB);
+      if (!mbar_wait(&bar[j], (unsigned)(last / WR_NB) & 1u, kDrainLimit)) atomicOr(a.status, DEV_TIMEOUT);
+    }
+  }
+}
+
 // Second pass of a segmented reduction: the carry into every tile is the
 // segmented exclusive scan of the tile aggregates (status TS_INC marks a
 // tile holding a segment start; its value is the fold from its last start);
@@ -1345,6 +1563,42 @@ bool run_scan_tma(typename Op::T *out, const typename Op::T *in, vec_p sd, int n
       GCVL_CK(cudaMemsetAsync(mem, 0, lookback_clear_bytes(tiles), S.stream));
       k_scan_ring<Op, SEG><<<grid, RTB, ring_smem<T>(), S.stream>>>(tin, tout, a, tiles);
       launch_check(name);
+      return true;
+    }
+  }
+  if constexpr (MODE == M_REDUCE && SEG && sizeof(T) == 4 && !std::is_same<Op, AddD>::value) {
+    if (GCVL_RED_WARP && (long)n >= RING_RED_MEAN * m) {
+      // per-warp ranges: as many as fit at once, at most one per chunk and
+      // no more than the tile form's tiles (whose scratch this shares)
+      const long chunks = ceil_div(n, (long)WR_ELEMS);
+      static int per_sm = -1;
+      if (per_sm < 0) {
+        per_sm = 0;
+        if (GCVL_CK(cudaFuncSetAttribute(k_segred_warp<Op>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)wr_smem())))
+          GCVL_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_segred_warp<Op>, WR_WARPS * 32,
+                                                                wr_smem()));
+      }
+      long ranges = (long)(per_sm > 0 ? per_sm : 1) * S.sm_count * WR_WARPS;
+      ranges = std::min(ranges, chunks);
+      ranges = std::min(ranges, (long)ceil_div(n, (long)TT * row_items<T>()));
+      if (ranges < 1) ranges = 1;
+      if (!tma_map<T>(&tin, in, rows, 32)) return false;
+      void *mem = scratch_or_work(scratch, reduce_pass_bytes((int)ranges));
+      if (!mem) return true;
+      TArgs<T> a{};
+      a.out = out; a.in = in; a.n = n; a.rows = rows;
+      a.sv = seg_view(sd, n, m);
+      a.lb = lookback_carve(mem, (int)ranges);
+      a.status = S.d_status;
+      a.spin_limit = S.spin_limit;
+      a.lead = (int *)((char *)a.lb.word + align_up((size_t)ranges * 16, 256));
+      if (!GCVL_CK(cudaMemsetAsync(mem, 0, lookback_clear_bytes((int)ranges), S.stream))) return true;
+      if (!GCVL_CK(cudaMemsetAsync(a.lead, 0xFF, (size_t)ranges * 4, S.stream))) return true;
+      k_segred_warp<Op><<<ceil_div(ranges, (long)WR_WARPS), WR_WARPS * 32, wr_smem(), S.stream>>>(tin, a, chunks,
+                                                                                               (int)ranges);
+      launch_check(name);
+      launch_tile_fix<Op>(a.lb.word, a.lead, (int)ranges, out);
       return true;
     }
   }

@@ -279,3 +279,30 @@ def test_default_permute_ascending_with_repeats(gpu, oracle, n):
     strict = np.concatenate([np.arange(L) for L in lens]).astype(np.int32)
     compare("exact", ops.dpe_e(gpu, "dpe_pez", x, strict, dflt, lens, lens),
             ops.dpe_e(oracle, "dpe_pez", x, strict, dflt, lens, lens))
+
+
+@pytest.mark.parametrize("shape", ["chunk-aligned", "empties", "ragged"])
+def test_reductions_per_warp_ranges(gpu, oracle, shape):
+    """4-byte segmented reductions with segments averaging 32 elements or
+    more run along per-warp ranges of 1024-element chunks: segment ends on
+    chunk boundaries, runs of empty segments longer than one 32-segment
+    round (and leading and trailing ones), a length off every chunk and row
+    boundary, every operator, against the oracle."""
+    r = W.rng({"chunk-aligned": 1, "empties": 2, "ragged": 3}[shape])
+    if shape == "chunk-aligned":
+        lens = np.full(3000, 1024, dtype=np.int32)
+        lens[::7] = 2048
+    elif shape == "empties":
+        base = W.geometric_lengths(r, 1_500_000, 300.0)
+        lens = np.concatenate([np.zeros(5, np.int32), base[:100], np.zeros(40, np.int32), base[100:],
+                               np.zeros(37, np.int32)]).astype(np.int32)
+    else:
+        lens = W.with_empty(r, W.geometric_lengths(r, 1024 * 777 + 29, 64.0), 0.1)
+    n = int(lens.sum())
+    xi = r.integers(-1000, 1000, size=n).astype(np.int32)
+    xb = (r.random(n) < 0.7).astype(np.int32)
+    for name in ("add_rez", "mul_rez", "min_rez", "max_rez", "and_rez", "ior_rez", "xor_rez"):
+        compare("exact", ops.reduce_e(gpu, name, xi, lens), ops.reduce_e(oracle, name, xi, lens))
+    for name in ("and_reb", "ior_reb", "xor_reb"):
+        compare("exact", ops.reduce_e(gpu, name, xb, lens), ops.reduce_e(oracle, name, xb, lens))
+    compare("exact", ops.pk1_e(gpu, xb, lens), ops.pk1_e(oracle, xb, lens))
