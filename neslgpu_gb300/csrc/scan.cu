@@ -1189,8 +1189,11 @@ constexpr unsigned WR_CHUNK_BYTES = WR_ELEMS * 4;
 constexpr size_t wr_warp_bytes() { return (size_t)WR_NB * WR_CHUNK_BYTES; }
 constexpr size_t wr_smem() { return 1024 + WR_WARPS * wr_warp_bytes(); }
 
+#ifndef GCVL_WR_MINB
+#define GCVL_WR_MINB 6
+#endif
 template <class Op>
-__global__ void __launch_bounds__(WR_WARPS * 32)
+__global__ void __launch_bounds__(WR_WARPS * 32, GCVL_WR_MINB)
     k_segred_warp(const __grid_constant__ CUtensorMap tin, TArgs<typename Op::T> a, long chunks, int ranges) {
   typedef typename Op::T T;
   static_assert(sizeof(T) == 4, "rows of 32 four-byte elements");
@@ -1279,38 +1282,36 @@ __global__ void __launch_bounds__(WR_WARPS * 32)
     if (k0 + cnt >= n) nb = 1u;
     const unsigned ends =
         cnt == 0 ? 0u : (((heads >> 1) | (nb << (cnt - 1))) & (cnt >= 32 ? ~0u : ((1u << cnt) - 1u)));
-    // One pass over the row: the value at every segment end whose segment
-    // starts in the row is final and recorded at once; the row's first end,
-    // when its segment began before the row, waits for the lanes' prefix;
-    // what remains is the row's open piece (fold since its last head).
+    // One pass over the row: the running value of every item (restarting at
+    // each head), all 32 stored with 16-byte stores at the row's swizzled
+    // place; the values at segment ends whose segment starts in the row are
+    // final, the row's first end before its first head waits for the lanes'
+    // prefix.  r ends as the row's open piece (fold since its last head).
     T r = Op::ident();
-    bool started = false;
-    T first_v = Op::ident();
-    int first_p = -1;
-    const int pbase = lane * 32;
+    T y[32];
     if (cnt == 32) {
 #pragma unroll
       for (int i = 0; i < 32; i++) {
-        if ((heads >> i) & 1u) { r = Op::apply(Op::init(), x[i]); started = true; }
-        else r = Op::apply(r, x[i]);
-        if ((ends >> i) & 1u) {
-          if (started) s_end[pbase + i] = r;
-          else { first_v = r; first_p = pbase + i; }
-        }
+        r = ((heads >> i) & 1u) ? Op::apply(Op::init(), x[i]) : Op::apply(r, x[i]);
+        y[i] = r;
       }
     } else {
 #pragma unroll
       for (int i = 0; i < 32; i++) {
-        if (i < cnt) {
-          if ((heads >> i) & 1u) { r = Op::apply(Op::init(), x[i]); started = true; }
-          else r = Op::apply(r, x[i]);
-          if ((ends >> i) & 1u) {
-            if (started) s_end[pbase + i] = r;
-            else { first_v = r; first_p = pbase + i; }
-          }
-        }
+        if (i < cnt) r = ((heads >> i) & 1u) ? Op::apply(Op::init(), x[i]) : Op::apply(r, x[i]);
+        y[i] = r;
       }
     }
+    unsigned char *s_row = (unsigned char *)s_end + lane * 128;
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+      uint4 u;
+      memcpy(&u, &y[4 * q], 16);
+      *(uint4 *)(s_row + (((q ^ lane) & 7) << 4)) = u;
+    }
+    const bool started = heads != 0;
+    const int fh = started ? __ffs(heads) - 1 : 32, fe = ends ? __ffs(ends) - 1 : 32;
+    const int first_p = fe < fh ? lane * 32 + fe : -1;  // the first end, before any head
     // the lanes' segmented scan of their open pieces, the value entering each row
     int f = started;
     T v = r;
@@ -1324,7 +1325,8 @@ __global__ void __launch_bounds__(WR_WARPS * 32)
     T ev = shfl_up(v, 1);
     if (lane == 0) { ef = 0; ev = Op::ident(); }
     if (first_p >= 0) {
-      s_end[first_p] = Op::apply(ef ? ev : Op::apply(wc, ev), first_v);
+      T *slot = (T *)(s_row + ((((fe >> 2) ^ lane) & 7) << 4)) + (fe & 3);
+      *slot = Op::apply(ef ? ev : Op::apply(wc, ev), *slot);
       if (!ef && !wh) lead_l = -2 - first_p;  // marks the position; the segment is named below
     }
     const int lf = __shfl_sync(0xffffffffu, f, 31);
@@ -1347,8 +1349,9 @@ __global__ void __launch_bounds__(WR_WARPS * 32)
         if (po == o) {
           a.out[sg] = Op::init();  // an empty segment
         } else {
-          const int pe = (int)((long)o - 1 - cs);
-          a.out[sg] = s_end[pe];
+          const int pe = (int)((long)o - 1 - cs);  // row pe / 32, item pe % 32, swizzled as written
+          a.out[sg] = *((const T *)((const unsigned char *)s_end + (pe >> 5) * 128 +
+                                    ((((pe & 31) >> 2) ^ (pe >> 5)) & 7) * 16) + (pe & 3));
           if (pe == ipos) lead_l = sg;
         }
       }
