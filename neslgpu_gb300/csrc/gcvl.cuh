@@ -286,9 +286,10 @@ inline LookbackMem lookback_carve(void *base, int tiles) {
 inline int lookback_units(int tiles) { return (int)((lookback_bytes(tiles) + 7) / 8); }
 
 // Partitioned scatter (rank.cu): d[idx[k]] = s[k] for k < n, idx in
-// [0, n_d), by a partition of (index, value) pairs into 256 windows of the
-// output and a window-by-window scatter.  Worth it once the output is larger
-// than L2 can absorb random writes to; scratch of scatter_partitioned_bytes.
+// [0, n_d), by a split of the (index, value) pairs into windows of the
+// output (at most 8 MB each) and a window-by-window scatter.  Worth it once
+// the output is larger than L2 can absorb random writes to; scratch of
+// scatter_partitioned_bytes.
 bool scatter_partitioned_wanted(long n_d, size_t vsize);
 size_t scatter_partitioned_bytes(long n, size_t vsize);
 template <class V> void scatter_partitioned(V *d, const V *s, const int *idx, int n, int n_d, vec_p scratch);

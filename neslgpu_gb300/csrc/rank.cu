@@ -138,29 +138,6 @@ __global__ void __launch_bounds__(RK_BLOCK) k_rank_prep(RankPrep p) {
     if (s_hist[i]) atomicAdd(&p.hist[i], s_hist[i]);
 }
 
-// histogram of one digit of 32-bit keys (the partition of a scatter); with
-// `unsorted` non-null it also records whether any key exceeds its successor
-__global__ void __launch_bounds__(RK_BLOCK) k_digit_hist(const unsigned *key, long n, int shift, unsigned *hist,
-                                                         unsigned *unsorted) {
-  __shared__ unsigned s_hist[256];
-  __shared__ int s_uns;
-  s_hist[threadIdx.x] = 0;
-  if (threadIdx.x == 0) s_uns = 0;
-  __syncthreads();
-  const long stride = (long)gridDim.x * RK_BLOCK;
-  int uns = 0;
-  for (long i = (long)blockIdx.x * RK_BLOCK + threadIdx.x; i < n; i += stride) {
-    const unsigned k = __ldcs(key + i);
-    atomicAdd(&s_hist[(k >> shift) & 255], 1u);
-    // the successor's load usually hits the line just read by the next lane
-    if (unsorted && i + 1 < n && k > __ldg(key + i + 1)) uns = 1;
-  }
-  if (unsorted && __any_sync(0xffffffffu, uns) && (threadIdx.x & 31) == 0) s_uns = 1;
-  __syncthreads();
-  if (s_hist[threadIdx.x]) atomicAdd(&hist[threadIdx.x], s_hist[threadIdx.x]);
-  if (threadIdx.x == 0 && s_uns) atomicOr(unsorted, 1u);
-}
-
 // d[idx[i]] = s[i] when the indices ascend (gate word zero): the stores of a
 // warp then fall on few lines, and no partition is needed
 template <class V>
@@ -228,7 +205,7 @@ template <class K, class V> struct PassArgs {
   int spin_limit;
 };
 
-template <class K, class V, bool AUX, bool STABLE = true> constexpr size_t pass_smem() {
+template <class K, class V, bool AUX> constexpr size_t pass_smem() {
   return (size_t)RK_TILE * (sizeof(K) + sizeof(V) + (AUX ? 4 : 0)) + RK_WARPS * 256 * 2 + 256 * 4 + 256 * 8;
 }
 
@@ -277,11 +254,10 @@ __device__ __forceinline__ unsigned bin_lookback(unsigned *state, int tile, int 
   return prefix;
 }
 
-// STABLE: equal digits keep their order (every pass of a rank).  A pass
-// that only groups pairs by output window (the partitioned scatter) need
-// not: its slots come from shared-memory atomics instead of ballots.
+// Equal digits keep their order (the ballots below rank each warp's
+// elements in element order).
 template <class K, bool AUX> constexpr int rk_minb() { return sizeof(K) == 4 && !AUX ? GCVL_RK_MINB_NARROW : GCVL_RK_MINB; }
-template <class K, class V, bool AUX, int IN, int OUT, bool STABLE = true>
+template <class K, class V, bool AUX, int IN, int OUT>
 __global__ void __launch_bounds__(RK_BLOCK, rk_minb<K, AUX>()) k_radix_pass(PassArgs<K, V> a) {
   typedef unsigned short CntT;  // per-warp digit counts (at most 32 * RK_ITEMS)
   // 32-bit keys and values leave the reorder as one 8-byte pair
@@ -343,20 +319,11 @@ __global__ void __launch_bounds__(RK_BLOCK, rk_minb<K, AUX>()) k_radix_pass(Pass
     const int e = wbase + c * 32 + lane;
     const int d = e < valid ? (int)((kr[c] >> a.shift) & 255) : -1;
     unsigned r = 0;
-    if constexpr (STABLE) {
-      const unsigned peers = warp_match8(d);
-      if (d >= 0) r = cnt[d] + __popc(peers & lt);
-      __syncwarp();
-      if (d >= 0 && (peers & lt) == 0) cnt[d] = (CntT)(cnt[d] + __popc(peers));
-      __syncwarp();
-    } else {
-      // a slot from a shared-memory atomic on the 32-bit word holding the
-      // digit's 16-bit count
-      if (d >= 0) {
-        const unsigned sh = (d & 1) * 16;
-        r = (atomicAdd((unsigned *)(cnt + (d & ~1)), 1u << sh) >> sh) & 0xFFFFu;
-      }
-    }
+    const unsigned peers = warp_match8(d);
+    if (d >= 0) r = cnt[d] + __popc(peers & lt);
+    __syncwarp();
+    if (d >= 0 && (peers & lt) == 0) cnt[d] = (CntT)(cnt[d] + __popc(peers));
+    __syncwarp();
     wr[c] = d >= 0 ? (r << 8) | (unsigned)d : 0xFFFFFFFFu;
   }
   __syncthreads();
@@ -749,16 +716,16 @@ __global__ void __launch_bounds__(RK_BLOCK) k_gather_gated(V *__restrict__ d, co
   }
 }
 
-template <class K, class V, bool AUX, int IN, int OUT, bool STABLE = true>
+template <class K, class V, bool AUX, int IN, int OUT>
 void launch_pass(const PassArgs<K, V> &a, int tiles) {
-  constexpr size_t sm = pass_smem<K, V, AUX, STABLE>();
+  constexpr size_t sm = pass_smem<K, V, AUX>();
   static bool attr = false;
   if (!attr) {
-    GCVL_CK(cudaFuncSetAttribute(k_radix_pass<K, V, AUX, IN, OUT, STABLE>,
+    GCVL_CK(cudaFuncSetAttribute(k_radix_pass<K, V, AUX, IN, OUT>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     attr = true;
   }
-  k_radix_pass<K, V, AUX, IN, OUT, STABLE><<<tiles, RK_BLOCK, sm, stream()>>>(a);
+  k_radix_pass<K, V, AUX, IN, OUT><<<tiles, RK_BLOCK, sm, stream()>>>(a);
   launch_check("k_radix_pass");
 }
 

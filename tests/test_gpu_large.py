@@ -1,8 +1,10 @@
-"""Sizes past the point where rank and permute switch from a direct random
-scatter to the partitioned one (index/value pairs grouped into 256 windows
-of the output, then scattered window by window): results must stay
-bit-identical to the oracle there too.  Also the destination-longer-than-
-source case of the default permute, whose windows follow the destination."""
+"""Sizes past the point where rank, permute and gather switch from direct
+random accesses to partitioned ones (index/value pairs grouped by window of
+the output or the source, then scattered or gathered window by window):
+results must stay bit-identical to the oracle there too.  Also the
+destination-longer-than-source case of the default permute, whose windows
+follow the destination, and the segmented reductions' tile, ring and
+per-warp-range forms."""
 import numpy as np
 import pytest
 
