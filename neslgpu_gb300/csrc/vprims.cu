@@ -52,7 +52,13 @@ template <class F> void segwalk(F f, const SegView &sv, const char *name) {
 // per element (the segment, or the source address); phase 2 fetches all
 // the lane's values at once (independent loads in flight); the values pass
 // through shared memory so that every global load and store is coalesced.
-constexpr int SMI = 16, SMB = 128;
+#ifndef GCVL_SMI
+#define GCVL_SMI 16
+#endif
+#ifndef GCVL_SMB
+#define GCVL_SMB 128
+#endif
+constexpr int SMI = GCVL_SMI, SMB = GCVL_SMB;
 template <class F>
 __global__ void __launch_bounds__(SMB) k_segmap(F f, SegView sv) {
   typedef typename F::T T;
