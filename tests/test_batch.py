@@ -61,3 +61,27 @@ def test_modes_agree_and_match_oracle(gpu, oracle, is_double):
     assert np.all((ra["idx"] >= 0) & (ra["idx"] < newlens[seg]))
     for r in (ra, rp):
         compare("exact", r["g"], r["p"][off[seg] + r["idx"]])
+
+
+@pytest.mark.parametrize("is_double", [False, True])
+def test_skewed_batch_flattened_matches_percall(gpu, is_double):
+    """A few large vectors beside hundreds of tiny ones (the flattened
+    form's worst case): the flattened sequence and the per-vector loop give
+    the same results."""
+    b = B.make_skewed_batch(huge=2, huge_len=1 << 15, tiny=400, tiny_hi=60, seed=8)
+    run = B.BatchRun(b, is_double, cvl=gpu.cvl)
+    try:
+        n2a = run.batched()
+        ra = run.results(n2a)
+        n2p = run.percall()
+        rp = run.results(n2p)
+    finally:
+        run.free()
+    assert n2a == n2p
+    for k in ("f", "newlens", "idx"):
+        compare("exact", rp[k], ra[k])
+    for k in ("y", "p", "g"):
+        if is_double:  # float64 scans of the flattened vector reassociate only
+            np.testing.assert_allclose(rp[k], ra[k], rtol=1e-12, atol=1e-9)
+        else:
+            compare("exact", rp[k], ra[k])
