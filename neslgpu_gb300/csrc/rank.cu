@@ -62,7 +62,12 @@ constexpr int RK_MAXPASS = 12;
 #endif
 constexpr int RK_LB = GCVL_RK_LB;  // predecessors read per look-back round trip
 constexpr int RK_DIRECT_MAX = 1 << 23;
-constexpr int SC_ITEMS = 8;  // elements per thread in the streaming scatter
+// 8 measured best at 2^28 (bck_puz / smp_puz): 4 items 2.87 / 2.94 ms,
+// 8 items 2.63 / 2.78, 16 items 3.01 / 2.78
+#ifndef GCVL_SC_ITEMS
+#define GCVL_SC_ITEMS 8
+#endif
+constexpr int SC_ITEMS = GCVL_SC_ITEMS;  // elements per thread in the window and streaming passes
 constexpr unsigned RK_INC = 0x80000000u;
 
 // where a pass gets its tile from, and where it puts it
