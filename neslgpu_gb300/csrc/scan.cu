@@ -13,9 +13,13 @@
 //    tiles from a ticket counter, move them by TMA through a two-slot ring,
 //    and write each tile's outputs one round after its fold, so the carry
 //    it needs is ready;
-//  * k_scan_tma -- reductions of 16-byte aligned vectors, one TMA tile per
-//    CTA, results at segment ends and no look-back wait: k_tile_fix
-//    completes the results that span tiles (and the no-alloc scan);
+//  * k_segred_warp -- segmented reductions of 4-byte elements with segments
+//    of 32 elements or more on average: each warp streams its own range of
+//    chunks, the carry in registers, no look-back;
+//  * k_scan_tma -- the other reductions of 16-byte aligned vectors, one TMA
+//    tile per CTA, results at segment ends and no look-back wait:
+//    k_tile_fix completes the results that span tiles or warp ranges (and
+//    the no-alloc scan);
 //  * k_scan -- everything else (vectors off a 16-byte boundary, the offsets
 //    scan of mke_fov), staged with coalesced loads.
 // Every wait is bounded.
