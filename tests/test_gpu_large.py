@@ -308,3 +308,31 @@ def test_reductions_per_warp_ranges(gpu, oracle, shape):
     for name in ("and_reb", "ior_reb", "xor_reb"):
         compare("exact", ops.reduce_e(gpu, name, xb, lens), ops.reduce_e(oracle, name, xb, lens))
     compare("exact", ops.pk1_e(gpu, xb, lens), ops.pk1_e(oracle, xb, lens))
+
+
+@pytest.mark.parametrize("shape", ["geometric", "empties", "one", "ragged"])
+@pytest.mark.parametrize("t", ["z", "b", "d"])
+def test_distribute_per_warp_ranges(gpu, oracle, shape, t):
+    """DIST (dis_ve*) at large sizes: runs of empty segments, a single
+    huge segment, a ragged length, an output off a 16-byte boundary,
+    against the oracle."""
+    r = W.rng({"geometric": 11, "empties": 12, "one": 13, "ragged": 14}[shape])
+    if shape == "geometric":
+        lens = W.with_empty(r, W.geometric_lengths(r, 1 << 21, 64.0), 0.1)
+    elif shape == "empties":
+        base = W.geometric_lengths(r, 1 << 20, 200.0)
+        lens = np.concatenate([np.zeros(3, np.int32), base[:50], np.zeros(70, np.int32), base[50:],
+                               np.zeros(45, np.int32)]).astype(np.int32)
+    elif shape == "one":
+        lens = np.array([(1 << 20) + 3], dtype=np.int32)
+    else:
+        lens = W.geometric_lengths(r, 1024 * 333 + 7, 20.0)
+    m = len(lens)
+    vals = {"z": r.integers(-2 ** 31, 2 ** 31, size=m, dtype=np.int64).astype(np.int32),
+            "b": (r.random(m) < 0.5).astype(np.int32), "d": W.float64_normal(r, m)}[t]
+    want = ops.dis_e(oracle, f"dis_ve{t}", vals, lens)
+    compare("exact", ops.dis_e(gpu, f"dis_ve{t}", vals, lens), want)
+    if shape == "geometric":
+        from neslgpu_gb300.cvl import load
+        from neslgpu_gb300.ops import DeviceRunner
+        compare("exact", ops.dis_e(DeviceRunner(load(), offset=1), f"dis_ve{t}", vals, lens), want)
