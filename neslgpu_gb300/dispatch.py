@@ -7,7 +7,8 @@ segment (two chunk sizes) and, for ranks, a per-segment shared-memory rank.
 Which one is fastest depends on the segment-length distribution.
 
 * ``autotune`` times every valid variant of one call and returns the
-  fastest -- the dispatcher's fallback and its judge.
+  fastest -- the dispatcher's fallback, and the optimum its regret is
+  measured against.
 * ``sweep`` builds the training set: seeded synthetic descriptors
   (uniform, geometric, power-law and bimodal length distributions, totals
   log-uniform in [2^lo, 2^hi], int32 / uint32 / float64, scan / reduce /
